@@ -1,0 +1,208 @@
+/*
+ * mdrl.h — C ABI of libmdrl, a GB300 (sm_103a) implementation of the range-limited (RL)
+ * non-bonded force path of the SC2019-MD design: cell-list binning, half-shell pair generation
+ * (home cell + 13 neighbour cells), the 0 < r2 <= rc2 filter, LJ r^-14 / r^-8 plus Coulomb r^-3
+ * from interpolation tables indexed by the r2 bit pattern, Newton's-third-law force accumulation
+ * in deterministic int64 fixed point, and the motion update.
+ *
+ * Plain C: pointers, sizes and status codes only.  Every call returns an mdrl_status; the text
+ * of the last error on the calling thread is available from mdrl_last_error().  No call exits the
+ * process or throws across the ABI.
+ *
+ * Threading: one context per host thread.  Calls on one context are serialised by the caller;
+ * distinct contexts may be used concurrently from different threads (each owns its own CUDA
+ * stream and device buffers).
+ *
+ * Reference interfaces replaced (paths within the reference project):
+ *   int MD_Evaluation_Model()                 Range_Limited/C_Model_ForceEval/MD_Evaluation_Model.h:1
+ *                                             (.cpp:9-205)  -> MD_Evaluation_Model() below
+ *   float4 RL_LJ_Evaluation(int2, float4, float4)
+ *                                             Range_Limited_demo/SourceCode/OpenCL_HDL_Lib/
+ *                                             RL_LJ_Evaluation.h:1 (.xml:5-45)  -> mdrl_pair_eval
+ *   the RL force path of the MATLAB golden model
+ *                                             MatlabScripts/FullScale_Simulation_LJArgon.m:356-1164
+ *                                             -> mdrl_force_eval / mdrl_step
+ */
+#ifndef MDRL_H
+#define MDRL_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDRL_MAX_TYPES 16
+
+typedef enum {
+    MDRL_OK = 0,
+    MDRL_ERR_INVALID_ARG = 1,   /* a parameter or input failed validation */
+    MDRL_ERR_CELL_OVERFLOW = 2, /* a cell holds more particles than the kernels can stage */
+    MDRL_ERR_RANGE = 3,         /* rc > L/2, fewer than 3 cells per dimension, table range */
+    MDRL_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+    MDRL_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+    MDRL_ERR_STATE = 6          /* call order: e.g. mdrl_step before mdrl_set_state */
+} mdrl_status;
+
+/* Force accumulation. */
+enum {
+    MDRL_ACC_FIXED64 = 0,   /* FP32 partial sums in a fixed traversal order, int64 2^-24 atomics:
+                               bit-reproducible run to run */
+    MDRL_ACC_FP32_ATOMIC = 1, /* FP32 atomics ("plain"): order-dependent rounding */
+    MDRL_ACC_KAHAN = 2      /* compensated FP32 partial sums, then int64 fixed point */
+};
+
+/* Per-pair arithmetic. */
+enum {
+    MDRL_ARITH_FMA = 0,      /* c1*r2 + c0 and the force combination as fused multiply-adds */
+    MDRL_ARITH_SEPARATE = 1  /* every multiply and add rounded separately, as the reference's
+                                golden vectors (MATLAB polyval in single precision) */
+};
+
+/* Pair function evaluation. */
+enum {
+    MDRL_EVAL_TABLE = 0,  /* polynomial tables indexed by the r2 bit pattern */
+    MDRL_EVAL_DIRECT = 1  /* FP32 powers of 1/r2 */
+};
+
+/* Motion update. */
+enum {
+    MDRL_INT_VELOCITY_VERLET = 0, /* kick(dt/2) drift(dt) rebin force kick(dt/2) */
+    MDRL_INT_EULER = 1            /* v += a dt; x += v dt (the reference's symplectic Euler,
+                                     MD_Evaluation_Model.cpp:133-150,164-202) */
+};
+
+/* Flags. */
+#define MDRL_FLAG_ENERGY 0x1u      /* evaluate LJ / Coulomb energy and the virial every step */
+#define MDRL_FLAG_PAIR_COUNTS 0x2u /* count partners per particle (pair-list parity) */
+#define MDRL_FLAG_NO_PBC 0x4u      /* no periodic wrap of pair differences (mdrl_pair_eval) */
+
+typedef struct {
+    double box[3];         /* periodic box edges, Angstrom; positions live in [0, box) */
+    double cutoff;         /* rc, Angstrom; pairs with 0 < r2 <= rc^2 interact */
+    int ncell[3];          /* cells per dimension; 0 = floor(box / cutoff) */
+    int ntypes;            /* 1..MDRL_MAX_TYPES */
+    double sigma[MDRL_MAX_TYPES];   /* Angstrom */
+    double epsilon[MDRL_MAX_TYPES]; /* kcal/mol */
+    double mass[MDRL_MAX_TYPES];    /* amu */
+    double coulomb_k;      /* kcal*Angstrom/(mol*e^2); 0 = LJ only */
+    int table_order;       /* 1..3 (polynomial order of each bin) */
+    int table_bins;        /* bins per power-of-two segment: power of two, 16..4096 */
+    int table_min_log2;    /* the first segment starts at r2 = 2^table_min_log2 */
+    int eval;              /* MDRL_EVAL_* */
+    int arith;             /* MDRL_ARITH_* */
+    int accum;             /* MDRL_ACC_* */
+    int integrator;        /* MDRL_INT_* */
+    double dt_fs;          /* time step, fs */
+    uint32_t flags;        /* MDRL_FLAG_* */
+    int device;            /* CUDA device ordinal */
+} mdrl_params;
+
+typedef struct {
+    int64_t pairs;          /* unique pairs with 0 < r2 <= rc2 in the last force evaluation */
+    int64_t candidates;     /* candidate pairs tested by the half-shell traversal */
+    int64_t below_table;    /* pairs evaluated at the first table point (r2 below the table) */
+    int max_cell_occupancy;
+    int ncells;
+    double e_lj, e_coul;    /* kcal/mol (MDRL_FLAG_ENERGY) */
+    double virial;          /* sum over pairs of fscal*r2, kcal/mol (MDRL_FLAG_ENERGY) */
+    double kinetic;         /* kcal/mol, after the last step */
+    double device_ms;       /* device time of the last call, CUDA events */
+    int64_t pairs_total;    /* pairs summed over every force evaluation of the last call */
+    double force_ms;        /* device time of the last half-shell force kernel, CUDA events */
+} mdrl_stats;
+
+typedef struct mdrl_ctx mdrl_ctx;
+
+/* Library identity and the last error text of the calling thread ("" when none). */
+const char *mdrl_version(void);
+const char *mdrl_last_error(void);
+
+/* Fill *p with defaults: 1 type of argon (sigma 3.4, epsilon 0.238, 39.95 amu), rc 8.5,
+ * first-order 256-bin tables from 2^-2, FMA arithmetic, fixed-point accumulation,
+ * velocity Verlet at 2 fs, device 0. */
+void mdrl_default_params(mdrl_params *p);
+
+/* Fit the unit-prefactor tables on the host in FP64 (no GPU needed): coef receives 6 functions
+ * (r^-14, r^-8, r^-3, r^-12, r^-6, r^-1 as powers of r2) x (order+1) planes x nseg*bins, plane k
+ * holding the coefficient of r2^k of each bin's least-squares polynomial through `samples`
+ * equally spaced points (the reference uses 8). */
+mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples, float *coef);
+
+/* Create / destroy a context.  Validates the parameters, builds the FP64-fitted tables and
+ * uploads them; device buffers for particles are sized on first use. */
+mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out);
+mdrl_status mdrl_destroy(mdrl_ctx *ctx);
+
+/* Replace the generated tables, e.g. with the reference's ROM images.  coef holds nfunc
+ * functions (2: r^-14, r^-8; 3: + r^-3; 6: + r^-12, r^-6, r^-1), each as (order+1) planes of
+ * nseg*bins coefficients, plane k holding the coefficient of r2^k.  When raw_coefficients is
+ * nonzero the tables already carry their physical prefactors (as the reference's do) and the
+ * per-type multipliers become A = 1, B = -1, ke*qi*qj unchanged. */
+mdrl_status mdrl_set_tables(mdrl_ctx *ctx, int order, int nseg, int bins, int min_log2, int nfunc,
+                            const float *coef, int raw_coefficients);
+
+/* Read back the tables in use (same layout as mdrl_set_tables with nfunc = 6).  Pass coef = NULL
+ * to query the sizes. */
+mdrl_status mdrl_get_tables(mdrl_ctx *ctx, int *order, int *nseg, int *bins, int *min_log2,
+                            float *coef);
+
+/* Read back the per-type-pair multipliers in use: [ntypes*ntypes*4] = A14, B8, A12, B6 with the
+ * B terms negative (A14 = 48*eps*sig^12, B8 = -24*eps*sig^6, A12 = 4*eps*sig^12,
+ * B6 = -4*eps*sig^6, Lorentz-Berthelot mixing). */
+mdrl_status mdrl_get_pair_coefficients(mdrl_ctx *ctx, float *coef);
+
+/* Cell-list binning only (host arrays).  cell_of[n]: cell of each particle,
+ * (cx*ny + cy)*nz + cz with c = floor(x / (box/ncell)); cell_count[ncells]; order[n]: particle
+ * ids cell by cell, each cell in input order.  Any output may be NULL. */
+mdrl_status mdrl_bin(mdrl_ctx *ctx, int n, const float *x, const float *y, const float *z,
+                     int *cell_of, int *cell_count, int *order);
+
+/* One force evaluation on host arrays (copies in, evaluates, copies out).  q may be NULL
+ * (neutral), type may be NULL (all type 0).  counts[n] (optional) receives each particle's
+ * partner count; it requires no flag.  stats may be NULL. */
+mdrl_status mdrl_force_eval(mdrl_ctx *ctx, int n, const float *x, const float *y, const float *z,
+                            const float *q, const int *type, float *fx, float *fy, float *fz,
+                            int *counts, mdrl_stats *stats);
+
+/* The same on device arrays, enqueued on the context's stream and synchronised before return. */
+mdrl_status mdrl_force_eval_device(mdrl_ctx *ctx, int n, const float *x, const float *y,
+                                   const float *z, const float *q, const int *type, float *fx,
+                                   float *fy, float *fz, int *counts, mdrl_stats *stats);
+
+/* Per-pair evaluation, the drop-in for RL_LJ_Evaluation(particle_id, reference_pos,
+ * neighbor_pos): for each k < n, ref[4k..4k+3] = (x, y, z, q) and nbr likewise; out[4k..4k+3] =
+ * (Fx, Fy, Fz, 0), zero when the pair fails the filter.  type_ref / type_nbr may be NULL (type
+ * 0).  aux (optional) [2n] receives (r2, fscal) for every pair.  Host arrays. */
+mdrl_status mdrl_pair_eval(mdrl_ctx *ctx, int n, const float *ref, const float *nbr,
+                           const int *type_ref, const int *type_nbr, float *out, float *aux);
+
+/* Molecular dynamics on device-resident state.  set_state copies n particles in (velocities
+ * may be NULL: zero); step advances nsteps with the configured integrator, rebinning every
+ * step; get_state copies positions, velocities and the last forces out in the original particle
+ * order (any pointer may be NULL). */
+mdrl_status mdrl_set_state(mdrl_ctx *ctx, int n, const float *x, const float *y, const float *z,
+                           const float *vx, const float *vy, const float *vz, const float *q,
+                           const int *type);
+mdrl_status mdrl_step(mdrl_ctx *ctx, int nsteps, mdrl_stats *stats);
+mdrl_status mdrl_get_state(mdrl_ctx *ctx, float *x, float *y, float *z, float *vx, float *vy,
+                           float *vz, float *fx, float *fy, float *fz);
+
+/* Drop-in for the reference C model's entry point.  Reads the argon PDB named by the
+ * environment variable MDRL_INPUT (N from MDRL_N, default 500; iterations from MDRL_ITERS,
+ * default 100), runs the reference's all-pairs direct FP32 force and symplectic-Euler update on
+ * the GPU with the reference's constants and rounding, and prints
+ * "Iteration %d, System energy is %f, Kinetic Energy is %f" per iteration to stdout.
+ * Returns 1 on success and 0 on error (text in mdrl_last_error()). */
+int MD_Evaluation_Model(void);
+
+/* The same run with explicit arguments and no file or stdout: pos[3n] and vel[3n] are updated
+ * in place, energy[2*iters] receives (System_Energy, System_Kinetic_Energy) per iteration,
+ * counts[n] (optional) the partner counts of the last iteration. */
+mdrl_status mdrl_cmodel_run(int n, int iters, float box, float cutoff, float *pos, float *vel,
+                            float *energy, int *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDRL_H */

@@ -1,0 +1,33 @@
+"""Build the CPU oracle (oracle/_build/liboracle.so) from oracle.cpp.
+
+The oracle is test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline / reference arm load it.  -ffp-contract=off keeps every float expression rounded once
+per operation on x86-64 and aarch64 alike."""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_build"
+LIB = OUT / "liboracle.so"
+FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp"]
+
+
+def build(force: bool = False) -> Path:
+    srcs = [HERE / "oracle.cpp", HERE / "oracle.h"]
+    if not force and LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in srcs):
+        return LIB
+    OUT.mkdir(parents=True, exist_ok=True)
+    tmp = OUT / "liboracle.so.tmp"
+    cmd = ["g++", *FLAGS, str(HERE / "oracle.cpp"), "-o", str(tmp)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True))

@@ -1,0 +1,300 @@
+"""sc2019_md_gb300 — Python mirror of libmdrl's C ABI (include/mdrl.h).
+
+libmdrl is a GB300 (sm_103a) implementation of the SC2019-MD range-limited force path: cell
+binning, half-shell pairs, the 0 < r2 <= rc2 filter, tabulated LJ r^-14 / r^-8 plus Coulomb r^-3,
+Newton's-third-law accumulation in int64 fixed point and the motion update.  This module only
+marshals numpy arrays through ctypes; every computation runs in the CUDA library, and importing
+it fails loudly when the library has not been built (``python -m sc2019_md_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables",
+    "cmodel_run", "md_evaluation_model", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
+    "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
+    "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "MAX_TYPES", "STATUS",
+]
+
+MAX_TYPES = 16
+ACC_FIXED64, ACC_FP32_ATOMIC, ACC_KAHAN = 0, 1, 2
+ARITH_FMA, ARITH_SEPARATE = 0, 1
+EVAL_TABLE, EVAL_DIRECT = 0, 1
+INT_VELOCITY_VERLET, INT_EULER = 0, 1
+FLAG_ENERGY, FLAG_PAIR_COUNTS, FLAG_NO_PBC = 0x1, 0x2, 0x4
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CELL_OVERFLOW", 3: "RANGE", 4: "CUDA_ERROR",
+          5: "TIMEOUT", 6: "STATE"}
+
+_HERE = Path(__file__).resolve().parent
+
+
+def library_path() -> Path:
+    return _HERE / "_build" / "libmdrl.so"
+
+
+class MdrlError(RuntimeError):
+    """A libmdrl call returned a status other than MDRL_OK."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("box", C.c_double * 3), ("cutoff", C.c_double), ("ncell", C.c_int * 3),
+        ("ntypes", C.c_int), ("sigma", C.c_double * MAX_TYPES),
+        ("epsilon", C.c_double * MAX_TYPES), ("mass", C.c_double * MAX_TYPES),
+        ("coulomb_k", C.c_double), ("table_order", C.c_int), ("table_bins", C.c_int),
+        ("table_min_log2", C.c_int), ("eval", C.c_int), ("arith", C.c_int), ("accum", C.c_int),
+        ("integrator", C.c_int), ("dt_fs", C.c_double), ("flags", C.c_uint32), ("device", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("pairs", C.c_int64), ("candidates", C.c_int64), ("below_table", C.c_int64),
+        ("max_cell_occupancy", C.c_int), ("ncells", C.c_int), ("e_lj", C.c_double),
+        ("e_coul", C.c_double), ("virial", C.c_double), ("kinetic", C.c_double),
+        ("device_ms", C.c_double), ("pairs_total", C.c_int64), ("force_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int)
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libmdrl (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise ImportError(f"libmdrl is not built ({path}); run python -m sc2019_md_gb300.build")
+    L = C.CDLL(str(path))
+    st = C.c_int
+    vp = C.c_void_p
+    L.mdrl_version.restype = C.c_char_p
+    L.mdrl_last_error.restype = C.c_char_p
+    L.mdrl_default_params.argtypes = [C.POINTER(Params)]
+    L.mdrl_default_params.restype = None
+    L.mdrl_fit_tables.argtypes = [st, st, st, st, st, _F]
+    L.mdrl_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.mdrl_destroy.argtypes = [vp]
+    L.mdrl_set_tables.argtypes = [vp, st, st, st, st, st, _F, st]
+    L.mdrl_get_tables.argtypes = [vp, _I, _I, _I, _I, _F]
+    L.mdrl_get_pair_coefficients.argtypes = [vp, _F]
+    L.mdrl_bin.argtypes = [vp, st, _F, _F, _F, _I, _I, _I]
+    L.mdrl_force_eval.argtypes = [vp, st, _F, _F, _F, _F, _I, _F, _F, _F, _I, C.POINTER(Stats)]
+    L.mdrl_force_eval_device.argtypes = [vp, st, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.POINTER(Stats)]
+    L.mdrl_pair_eval.argtypes = [vp, st, _F, _F, _I, _I, _F, _F]
+    L.mdrl_set_state.argtypes = [vp, st, _F, _F, _F, _F, _F, _F, _F, _I]
+    L.mdrl_step.argtypes = [vp, st, C.POINTER(Stats)]
+    L.mdrl_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
+    L.MD_Evaluation_Model.argtypes = []
+    L.MD_Evaluation_Model.restype = C.c_int
+    L.mdrl_cmodel_run.argtypes = [st, st, C.c_float, C.c_float, _F, _F, _F, _I]
+    for name in ("mdrl_fit_tables", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
+                 "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
+                 "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
+                 "mdrl_get_state", "mdrl_cmodel_run"):
+        getattr(L, name).restype = st
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise MdrlError(status, lib().mdrl_last_error().decode())
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(_F)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_I)
+
+
+def _f32(a, n=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if n is not None and a.shape[0] != n:
+        raise ValueError("array length mismatch")
+    return a
+
+
+def _i32(a, n=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    if n is not None and a.shape[0] != n:
+        raise ValueError("array length mismatch")
+    return a
+
+
+def default_params(**kw) -> Params:
+    """Params filled by mdrl_default_params, then overridden by keyword (sequences for the
+    per-type arrays and the box)."""
+    p = Params()
+    lib().mdrl_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k in ("box", "ncell", "sigma", "epsilon", "mass"):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def fit_tables(order: int, nseg: int, bins: int, min_log2: int, samples: int = 8) -> np.ndarray:
+    """FP64-fitted unit tables, shape (6, order+1, nseg*bins) (host only, no GPU)."""
+    out = np.zeros((6, order + 1, nseg * bins), dtype=np.float32)
+    _check(lib().mdrl_fit_tables(order, nseg, bins, min_log2, samples, _fp(out)))
+    return out
+
+
+class Context:
+    """One libmdrl context (a CUDA stream, device buffers and tables)."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self.params = params if params is not None else default_params(**kw)
+        self._h = C.c_void_p()
+        _check(lib().mdrl_create(C.byref(self.params), C.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().mdrl_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # tables ------------------------------------------------------------------------------
+    def tables(self) -> tuple[np.ndarray, dict]:
+        o, s, b, m = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib().mdrl_get_tables(self._h, C.byref(o), C.byref(s), C.byref(b), C.byref(m), None))
+        out = np.zeros((6, o.value + 1, s.value * b.value), dtype=np.float32)
+        _check(lib().mdrl_get_tables(self._h, None, None, None, None, _fp(out)))
+        return out, {"order": o.value, "nseg": s.value, "bins": b.value, "min_log2": m.value}
+
+    def set_tables(self, coef: np.ndarray, order: int, nseg: int, bins: int, min_log2: int,
+                   raw: bool = False) -> None:
+        coef = np.ascontiguousarray(coef, dtype=np.float32)
+        nfunc = coef.shape[0]
+        _check(lib().mdrl_set_tables(self._h, order, nseg, bins, min_log2, nfunc, _fp(coef), int(raw)))
+
+    def pair_coefficients(self) -> np.ndarray:
+        T = self.params.ntypes
+        out = np.zeros((T * T, 4), dtype=np.float32)
+        _check(lib().mdrl_get_pair_coefficients(self._h, _fp(out)))
+        return out
+
+    # evaluation --------------------------------------------------------------------------
+    def bin(self, x, y, z):
+        x, y, z = _f32(x), _f32(y), _f32(z)
+        n = x.shape[0]
+        nc = self.params.ncell
+        cell_of = np.zeros(n, np.int32)
+        order = np.zeros(n, np.int32)
+        ncells = self._ncells()
+        count = np.zeros(ncells, np.int32)
+        _check(lib().mdrl_bin(self._h, n, _fp(x), _fp(y), _fp(z), _ip(cell_of), _ip(count), _ip(order)))
+        return cell_of, count, order
+
+    def _ncells(self) -> int:
+        p = self.params
+        tot = 1
+        for d in range(3):
+            nc = p.ncell[d] if p.ncell[d] > 0 else int(np.floor(np.float64(np.float32(p.box[d])) /
+                                                               np.float64(np.float32(p.cutoff))))
+            tot *= nc
+        return tot
+
+    def force(self, x, y, z, q=None, type=None, counts: bool = False):
+        """One force evaluation; returns (F (n,3) float32, stats dict, counts or None)."""
+        x = _f32(x)
+        n = x.shape[0]
+        y, z, q, t = _f32(y, n), _f32(z, n), _f32(q, n), _i32(type, n)
+        fx, fy, fz = (np.zeros(n, np.float32) for _ in range(3))
+        cnt = np.zeros(n, np.int32) if counts else None
+        st = Stats()
+        _check(lib().mdrl_force_eval(self._h, n, _fp(x), _fp(y), _fp(z), _fp(q), _ip(t), _fp(fx),
+                                     _fp(fy), _fp(fz), _ip(cnt), C.byref(st)))
+        return np.stack([fx, fy, fz], axis=1), st.as_dict(), cnt
+
+    def pair_eval(self, ref, nbr, type_ref=None, type_nbr=None):
+        """Per-pair plugin: ref/nbr (n,4) float32 (x,y,z,q); returns (out (n,4), aux (n,2))."""
+        ref = np.ascontiguousarray(ref, dtype=np.float32)
+        nbr = np.ascontiguousarray(nbr, dtype=np.float32)
+        n = ref.shape[0]
+        out = np.zeros((n, 4), np.float32)
+        aux = np.zeros((n, 2), np.float32)
+        _check(lib().mdrl_pair_eval(self._h, n, _fp(ref), _fp(nbr), _ip(_i32(type_ref, n)),
+                                    _ip(_i32(type_nbr, n)), _fp(out), _fp(aux)))
+        return out, aux
+
+    # molecular dynamics ------------------------------------------------------------------
+    def set_state(self, x, y, z, v=None, q=None, type=None) -> None:
+        x = _f32(x)
+        n = x.shape[0]
+        y, z = _f32(y, n), _f32(z, n)
+        self._n = n
+        vx = vy = vz = None
+        if v is not None:
+            v = np.asarray(v, dtype=np.float32)
+            vx, vy, vz = (np.ascontiguousarray(v[:, k]) for k in range(3))
+        self._keep = (x, y, z, vx, vy, vz, _f32(q, n), _i32(type, n))
+        k = self._keep
+        _check(lib().mdrl_set_state(self._h, n, _fp(k[0]), _fp(k[1]), _fp(k[2]), _fp(k[3]),
+                                    _fp(k[4]), _fp(k[5]), _fp(k[6]), _ip(k[7])))
+
+    def step(self, nsteps: int = 1) -> dict:
+        st = Stats()
+        _check(lib().mdrl_step(self._h, nsteps, C.byref(st)))
+        return st.as_dict()
+
+    def state(self):
+        n = self._n
+        a = [np.zeros(n, np.float32) for _ in range(9)]
+        _check(lib().mdrl_get_state(self._h, *[_fp(v) for v in a]))
+        return (np.stack(a[0:3], 1), np.stack(a[3:6], 1), np.stack(a[6:9], 1))
+
+
+def cmodel_run(pos: np.ndarray, vel: np.ndarray, iters: int, box: float = 24.0,
+               cutoff: float = 8.0, counts: bool = False):
+    """The reference C model's run on the GPU (mdrl_cmodel_run); returns (pos, vel, energy
+    (iters,2), counts or None)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).copy()
+    vel = np.ascontiguousarray(vel, dtype=np.float32).copy()
+    n = pos.shape[0]
+    energy = np.zeros((max(iters, 1), 2), np.float32)
+    cnt = np.zeros(n, np.int32) if counts else None
+    _check(lib().mdrl_cmodel_run(n, iters, C.c_float(box), C.c_float(cutoff), _fp(pos), _fp(vel),
+                                 _fp(energy), _ip(cnt)))
+    return pos, vel, energy[:iters], cnt
+
+
+def md_evaluation_model() -> int:
+    """Call the drop-in int MD_Evaluation_Model() (reads MDRL_INPUT, prints to stdout)."""
+    return lib().MD_Evaluation_Model()

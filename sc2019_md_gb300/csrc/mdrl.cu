@@ -1,0 +1,843 @@
+/*
+ * mdrl.cu — host side of libmdrl: context, validation, buffer management, launches and the
+ * CUDA-graph step.  Kernels live in mdrl_kernels.cuh.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <mutex>
+#include <set>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mdrl_internal.h"
+#include "mdrl_kernels.cuh"
+
+using namespace mdrl;
+
+namespace mdrl {
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace mdrl
+
+#define MDRL_CUDA(call)                                                                   \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                \
+            return MDRL_ERR_CUDA;                                                         \
+        }                                                                                 \
+    } while (0)
+
+#define MDRL_TRY(expr)                         \
+    do {                                       \
+        mdrl_status s_ = (expr);               \
+        if (s_ != MDRL_OK) return s_;          \
+    } while (0)
+
+template <class T>
+static mdrl_status dalloc(T **p, size_t count) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+    if (count == 0) return MDRL_OK;
+    MDRL_CUDA(cudaMalloc((void **)p, sizeof(T) * count));
+    return MDRL_OK;
+}
+
+template <class T>
+static void dfree(T **p) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+}
+
+struct mdrl_ctx {
+    mdrl_params p;
+    Geom g;
+    int ncells = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evf0 = nullptr, evf1 = nullptr; /* around the force kernel */
+
+    /* tables */
+    int order = 1, nseg = 0, bins = 256, min_log2 = -2;
+    bool raw = false;
+    std::vector<float> tab;      /* canonical [6][order+1][nseg*bins] */
+    std::vector<float> pcoef;    /* [T*T*4] */
+    float ke = 0.0f;
+    float2 *d_f2 = nullptr, *d_e2 = nullptr;
+    float4 *d_f4 = nullptr, *d_e4 = nullptr;
+    float4 *d_pcoef = nullptr;
+    MassTab mt_half, mt_full;
+
+    /* particle buffers */
+    int cap = 0, n = 0;
+    float *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_uq = nullptr;
+    int *d_ut = nullptr;
+    float *d_ox = nullptr, *d_oy = nullptr, *d_oz = nullptr; /* user-order outputs */
+    float *d_ovx = nullptr, *d_ovy = nullptr, *d_ovz = nullptr;
+    int *d_ocnt = nullptr;
+    float4 *d_pos[2] = {nullptr, nullptr}, *d_vel[2] = {nullptr, nullptr};
+    int *d_type[2] = {nullptr, nullptr}, *d_id[2] = {nullptr, nullptr};
+    int cur = 0;
+    int *d_cell_of = nullptr, *d_slot = nullptr, *d_tmp = nullptr, *d_sorted = nullptr;
+    int *d_count = nullptr, *d_start = nullptr;
+    unsigned long long *d_F64 = nullptr;
+    float *d_F32 = nullptr;
+    int *d_cnt = nullptr;
+    UnitOut *d_unit = nullptr;
+    double *d_kepart = nullptr;
+    int kecap = 0;
+    DevTotals *d_tot = nullptr;
+    unsigned *d_err = nullptr;
+
+    /* pair-eval staging */
+    int pcap = 0;
+    float4 *d_pr = nullptr, *d_pn = nullptr, *d_pout = nullptr;
+    int *d_ptr = nullptr, *d_ptn = nullptr;
+    float2 *d_paux = nullptr;
+
+    /* state */
+    bool have_state = false;
+    cudaGraph_t graph[2] = {nullptr, nullptr};          /* one step from buffer slot k to 1-k */
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    int graph_n = -1;
+    bool graph_extra = false;
+};
+
+extern "C" const char *mdrl_version(void) { return "mdrl 0.1 (sm_103a)"; }
+
+extern "C" const char *mdrl_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" void mdrl_default_params(mdrl_params *p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->box[0] = p->box[1] = p->box[2] = 25.5;
+    p->cutoff = 8.5;
+    p->ntypes = 1;
+    p->sigma[0] = 3.4;
+    p->epsilon[0] = 0.238;
+    p->mass[0] = 39.95;
+    p->coulomb_k = 0.0;
+    p->table_order = 1;
+    p->table_bins = 256;
+    p->table_min_log2 = -2;
+    p->eval = MDRL_EVAL_TABLE;
+    p->arith = MDRL_ARITH_FMA;
+    p->accum = MDRL_ACC_FIXED64;
+    p->integrator = MDRL_INT_VELOCITY_VERLET;
+    p->dt_fs = 2.0;
+    p->flags = 0;
+    p->device = 0;
+}
+
+static int ilog2i(int v) { int l = 0; while ((1 << l) < v) ++l; return l; }
+
+static mdrl_status validate(const mdrl_params *p) {
+    char buf[256];
+    for (int d = 0; d < 3; ++d)
+        if (!(p->box[d] > 0.0) || !std::isfinite(p->box[d])) {
+            set_error("box edges must be positive and finite");
+            return MDRL_ERR_INVALID_ARG;
+        }
+    if (!(p->cutoff > 0.0) || !std::isfinite(p->cutoff)) {
+        set_error("cutoff must be positive");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->ntypes < 1 || p->ntypes > MDRL_MAX_TYPES) {
+        set_error("ntypes must be in 1..16");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    for (int t = 0; t < p->ntypes; ++t)
+        if (!(p->sigma[t] > 0) || !(p->epsilon[t] >= 0) || !(p->mass[t] > 0)) {
+            snprintf(buf, sizeof buf, "type %d: sigma and mass must be positive, epsilon >= 0", t);
+            set_error(buf);
+            return MDRL_ERR_INVALID_ARG;
+        }
+    if (p->table_order < 1 || p->table_order > 3) {
+        set_error("table_order must be 1, 2 or 3");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->table_bins < 16 || p->table_bins > 4096 || (p->table_bins & (p->table_bins - 1))) {
+        set_error("table_bins must be a power of two in 16..4096");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->table_min_log2 < -30 || p->table_min_log2 > 20) {
+        set_error("table_min_log2 out of range");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->eval != MDRL_EVAL_TABLE && p->eval != MDRL_EVAL_DIRECT) {
+        set_error("eval must be MDRL_EVAL_TABLE or MDRL_EVAL_DIRECT");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->arith != MDRL_ARITH_FMA && p->arith != MDRL_ARITH_SEPARATE) {
+        set_error("arith must be MDRL_ARITH_FMA or MDRL_ARITH_SEPARATE");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->accum < MDRL_ACC_FIXED64 || p->accum > MDRL_ACC_KAHAN) {
+        set_error("accum must be one of MDRL_ACC_*");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (p->integrator != MDRL_INT_VELOCITY_VERLET && p->integrator != MDRL_INT_EULER) {
+        set_error("integrator must be MDRL_INT_VELOCITY_VERLET or MDRL_INT_EULER");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (!(p->dt_fs > 0.0) || !std::isfinite(p->dt_fs)) {
+        set_error("dt_fs must be positive");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    return MDRL_OK;
+}
+
+/* Cell grid and geometry; RANGE when the half shell would be wrong (n < 3 or edge < rc). */
+static mdrl_status setup_geometry(mdrl_ctx *c) {
+    const mdrl_params &p = c->p;
+    const float rcf = (float)p.cutoff;
+    c->g.rc2 = rcf * rcf;
+    for (int d = 0; d < 3; ++d) {
+        const float L = (float)p.box[d];
+        int nc = p.ncell[d] > 0 ? p.ncell[d] : (int)std::floor((double)L / (double)rcf);
+        c->g.L[d] = L;
+        c->g.h[d] = 0.5f * L;
+        c->g.nc[d] = nc;
+        c->g.edge[d] = nc > 0 ? (float)((double)L / (double)nc) : 0.0f;
+    }
+    return MDRL_OK;
+}
+
+static mdrl_status check_cells(mdrl_ctx *c) {
+    char buf[256];
+    for (int d = 0; d < 3; ++d) {
+        if (c->g.nc[d] < 3) {
+            snprintf(buf, sizeof buf,
+                     "axis %d: %d cells; the half-shell traversal needs at least 3 cells of edge >= rc "
+                     "per axis (box %.4f, rc %.4f)", d, c->g.nc[d], (double)c->g.L[d], c->p.cutoff);
+            set_error(buf);
+            return MDRL_ERR_RANGE;
+        }
+        if ((double)c->g.edge[d] < (double)(float)c->p.cutoff) {
+            snprintf(buf, sizeof buf, "axis %d: cell edge %.6f is below the cutoff %.6f", d,
+                     (double)c->g.edge[d], c->p.cutoff);
+            set_error(buf);
+            return MDRL_ERR_RANGE;
+        }
+    }
+    const long long nc = (long long)c->g.nc[0] * c->g.nc[1] * c->g.nc[2];
+    if (nc > (1LL << 24) || nc * kHalfShellCells > 2147483647LL) {
+        set_error("too many cells");
+        return MDRL_ERR_RANGE;
+    }
+    return MDRL_OK;
+}
+
+static mdrl_status upload_tables(mdrl_ctx *c) {
+    const int nidx = c->nseg * c->bins;
+    const int nc = c->order + 1;
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4);
+    auto coef = [&](int f, int k, int idx) { return c->tab[((size_t)f * nc + k) * nidx + idx]; };
+    if (c->order == 1) {
+        std::vector<float2> f2((size_t)3 * nidx), e2((size_t)3 * nidx);
+        for (int i = 0; i < nidx; ++i)
+            for (int f = 0; f < 3; ++f) {
+                f2[(size_t)3 * i + f] = make_float2(coef(f, 0, i), coef(f, 1, i));
+                e2[(size_t)3 * i + f] = make_float2(coef(3 + f, 0, i), coef(3 + f, 1, i));
+            }
+        MDRL_TRY(dalloc(&c->d_f2, f2.size()));
+        MDRL_TRY(dalloc(&c->d_e2, e2.size()));
+        MDRL_CUDA(cudaMemcpy(c->d_f2, f2.data(), sizeof(float2) * f2.size(), cudaMemcpyHostToDevice));
+        MDRL_CUDA(cudaMemcpy(c->d_e2, e2.data(), sizeof(float2) * e2.size(), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float4> f4((size_t)3 * nidx), e4((size_t)3 * nidx);
+        for (int i = 0; i < nidx; ++i)
+            for (int f = 0; f < 3; ++f) {
+                float a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+                for (int k = 0; k < nc; ++k) { a[k] = coef(f, k, i); b[k] = coef(3 + f, k, i); }
+                f4[(size_t)3 * i + f] = make_float4(a[0], a[1], a[2], a[3]);
+                e4[(size_t)3 * i + f] = make_float4(b[0], b[1], b[2], b[3]);
+            }
+        MDRL_TRY(dalloc(&c->d_f4, f4.size()));
+        MDRL_TRY(dalloc(&c->d_e4, e4.size()));
+        MDRL_CUDA(cudaMemcpy(c->d_f4, f4.data(), sizeof(float4) * f4.size(), cudaMemcpyHostToDevice));
+        MDRL_CUDA(cudaMemcpy(c->d_e4, e4.data(), sizeof(float4) * e4.size(), cudaMemcpyHostToDevice));
+    }
+    /* per-type-pair multipliers */
+    const int T = c->p.ntypes;
+    std::vector<float4> pc((size_t)T * T);
+    for (int k = 0; k < T * T; ++k) {
+        if (c->raw)
+            pc[k] = make_float4(1.0f, -1.0f, 1.0f, -1.0f);
+        else
+            pc[k] = make_float4(c->pcoef[4 * k], c->pcoef[4 * k + 1], c->pcoef[4 * k + 2], c->pcoef[4 * k + 3]);
+    }
+    MDRL_TRY(dalloc(&c->d_pcoef, pc.size()));
+    MDRL_CUDA(cudaMemcpy(c->d_pcoef, pc.data(), sizeof(float4) * pc.size(), cudaMemcpyHostToDevice));
+    return MDRL_OK;
+}
+
+static TableDev table_dev(const mdrl_ctx *c) {
+    TableDev t;
+    t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4;
+    t.order = c->order; t.nseg = c->nseg; t.bins = c->bins; t.lb = ilog2i(c->bins);
+    t.min_log2 = c->min_log2;
+    t.r2min = std::ldexp(1.0f, c->min_log2);
+    return t;
+}
+
+static int segments_for(float rc2, int min_log2) {
+    int e;
+    std::frexp(rc2, &e); /* rc2 = m * 2^e, m in [0.5, 1) -> floor(log2 rc2) = e - 1 */
+    return (e - 1) - min_log2 + 1;
+}
+
+extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
+    if (!p || !out) { set_error("null argument"); return MDRL_ERR_INVALID_ARG; }
+    *out = nullptr;
+    MDRL_TRY(validate(p));
+    int ndev = 0;
+    MDRL_CUDA(cudaGetDeviceCount(&ndev));
+    if (p->device < 0 || p->device >= ndev) { set_error("device ordinal out of range"); return MDRL_ERR_INVALID_ARG; }
+    MDRL_CUDA(cudaSetDevice(p->device));
+    mdrl_ctx *c = new mdrl_ctx();
+    c->p = *p;
+    setup_geometry(c);
+    c->order = p->table_order;
+    c->bins = p->table_bins;
+    c->min_log2 = p->table_min_log2;
+    c->nseg = segments_for(c->g.rc2, c->min_log2);
+    if (c->nseg < 1) {
+        delete c;
+        set_error("cutoff lies below the first table segment");
+        return MDRL_ERR_RANGE;
+    }
+    c->ke = (float)p->coulomb_k;
+    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab);
+    mix_pair_coefficients(*p, &c->pcoef, nullptr);
+    const double conv = 4.184e-4; /* (kcal/mol/A)/amu -> A/fs^2 */
+    for (int t = 0; t < MDRL_MAX_TYPES; ++t) {
+        const double m = t < p->ntypes ? p->mass[t] : 1.0;
+        c->mt_half.cm[t] = (float)(0.5 * p->dt_fs * conv / m);
+        c->mt_full.cm[t] = (float)(p->dt_fs * conv / m);
+        c->mt_half.mass[t] = c->mt_full.mass[t] = (float)m;
+    }
+    mdrl_status s = upload_tables(c);
+    if (s != MDRL_OK) { mdrl_destroy(c); return s; }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->evf0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->evf1);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_tot, sizeof(DevTotals));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_err, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        set_error(std::string("context setup: ") + cudaGetErrorString(e));
+        mdrl_destroy(c);
+        return MDRL_ERR_CUDA;
+    }
+    *out = c;
+    return MDRL_OK;
+}
+
+static void free_particles(mdrl_ctx *c) {
+    dfree(&c->d_ux); dfree(&c->d_uy); dfree(&c->d_uz); dfree(&c->d_uq); dfree(&c->d_ut);
+    dfree(&c->d_ox); dfree(&c->d_oy); dfree(&c->d_oz);
+    dfree(&c->d_ovx); dfree(&c->d_ovy); dfree(&c->d_ovz); dfree(&c->d_ocnt);
+    for (int b = 0; b < 2; ++b) { dfree(&c->d_pos[b]); dfree(&c->d_vel[b]); dfree(&c->d_type[b]); dfree(&c->d_id[b]); }
+    dfree(&c->d_cell_of); dfree(&c->d_slot); dfree(&c->d_tmp); dfree(&c->d_sorted);
+    dfree(&c->d_F64); dfree(&c->d_F32); dfree(&c->d_cnt);
+    c->cap = 0;
+}
+
+extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
+    if (!c) return MDRL_OK;
+    cudaSetDevice(c->p.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int k = 0; k < 2; ++k) {
+        if (c->graph_exec[k]) cudaGraphExecDestroy(c->graph_exec[k]);
+        if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
+    }
+    free_particles(c);
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_pcoef);
+    dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
+    dfree(&c->d_tot); dfree(&c->d_err);
+    dfree(&c->d_pr); dfree(&c->d_pn); dfree(&c->d_pout); dfree(&c->d_ptr); dfree(&c->d_ptn); dfree(&c->d_paux);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->evf0) cudaEventDestroy(c->evf0);
+    if (c->evf1) cudaEventDestroy(c->evf1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MDRL_OK;
+}
+
+static mdrl_status ensure_cells(mdrl_ctx *c) {
+    if (c->ncells) return MDRL_OK;
+    MDRL_TRY(check_cells(c));
+    c->ncells = c->g.nc[0] * c->g.nc[1] * c->g.nc[2];
+    MDRL_TRY(dalloc(&c->d_count, c->ncells));
+    MDRL_TRY(dalloc(&c->d_start, c->ncells + 1));
+    MDRL_TRY(dalloc(&c->d_unit, (size_t)c->ncells * kHalfShellCells));
+    return MDRL_OK;
+}
+
+static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
+    MDRL_TRY(ensure_cells(c));
+    if (n <= c->cap) return MDRL_OK;
+    free_particles(c);
+    const size_t m = (size_t)n;
+    MDRL_TRY(dalloc(&c->d_ux, m)); MDRL_TRY(dalloc(&c->d_uy, m)); MDRL_TRY(dalloc(&c->d_uz, m));
+    MDRL_TRY(dalloc(&c->d_uq, m)); MDRL_TRY(dalloc(&c->d_ut, m));
+    MDRL_TRY(dalloc(&c->d_ox, m)); MDRL_TRY(dalloc(&c->d_oy, m)); MDRL_TRY(dalloc(&c->d_oz, m));
+    MDRL_TRY(dalloc(&c->d_ovx, m)); MDRL_TRY(dalloc(&c->d_ovy, m)); MDRL_TRY(dalloc(&c->d_ovz, m));
+    MDRL_TRY(dalloc(&c->d_ocnt, m));
+    for (int b = 0; b < 2; ++b) {
+        MDRL_TRY(dalloc(&c->d_pos[b], m)); MDRL_TRY(dalloc(&c->d_vel[b], m));
+        MDRL_TRY(dalloc(&c->d_type[b], m)); MDRL_TRY(dalloc(&c->d_id[b], m));
+    }
+    MDRL_TRY(dalloc(&c->d_cell_of, m)); MDRL_TRY(dalloc(&c->d_slot, m));
+    MDRL_TRY(dalloc(&c->d_tmp, m)); MDRL_TRY(dalloc(&c->d_sorted, m));
+    if (c->p.accum == MDRL_ACC_FP32_ATOMIC) { MDRL_TRY(dalloc(&c->d_F32, 3 * m)); }
+    else { MDRL_TRY(dalloc(&c->d_F64, 3 * m)); }
+    MDRL_TRY(dalloc(&c->d_cnt, m));
+    const int nke = (n + 255) / 256;
+    MDRL_TRY(dalloc(&c->d_kepart, nke));
+    c->kecap = nke;
+    c->cap = n;
+    c->have_state = false;
+    c->graph_n = -1; /* captured graphs hold the old buffer addresses */
+    return MDRL_OK;
+}
+
+/* ---- kernel dispatch ---------------------------------------------------------------------- */
+
+typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
+                         int, float, int, unsigned long long *, float *, int *, UnitOut *);
+
+template <int ORDER, bool SEP, bool EXTRA>
+static force_fn pick_acc(int acc) {
+    return acc == MDRL_ACC_FP32_ATOMIC ? (force_fn)k_force<ORDER, SEP, EXTRA, 1>
+                                       : (force_fn)k_force<ORDER, SEP, EXTRA, 0>;
+}
+
+template <int ORDER>
+static force_fn pick_sep(bool sep, bool extra, int acc) {
+    if (sep) return extra ? pick_acc<ORDER, true, true>(acc) : pick_acc<ORDER, true, false>(acc);
+    return extra ? pick_acc<ORDER, false, true>(acc) : pick_acc<ORDER, false, false>(acc);
+}
+
+static force_fn pick_force(int order, bool sep, bool extra, int acc) {
+    switch (order) {
+        case 0: return pick_sep<0>(sep, extra, acc);
+        case 1: return pick_sep<1>(sep, extra, acc);
+        case 2: return pick_sep<2>(sep, extra, acc);
+        default: return pick_sep<3>(sep, extra, acc);
+    }
+}
+
+static int eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
+
+static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra) {
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum);
+    const size_t smem = force_smem_bytes(c->p.ntypes);
+    {
+        /* The attribute is set once per kernel and device, outside any stream capture. */
+        static std::mutex mu;
+        static std::set<std::pair<const void *, int>> done;
+        std::lock_guard<std::mutex> lock(mu);
+        const std::pair<const void *, int> key((const void *)fn, c->p.device);
+        if (!done.count(key)) {
+            MDRL_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)force_smem_bytes(MDRL_MAX_TYPES)));
+            done.insert(key);
+        }
+    }
+    const int units = c->ncells * kHalfShellCells;
+    MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
+    fn<<<units, kThreads, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
+                                              c->p.ntypes, c->ke, n, c->d_F64, c->d_F32, c->d_cnt,
+                                              c->d_unit);
+    MDRL_CUDA(cudaGetLastError());
+    MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
+    return MDRL_OK;
+}
+
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+/* Bin user-order arrays (already on the device) into the sorted buffers of slot `buf`. */
+static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                            const float *q, const int *type, int buf) {
+    MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
+    MDRL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+    if (n > 0) {
+        k_bin_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, x, y, z, c->g, c->d_cell_of, c->d_slot,
+                                                        c->d_count, c->d_err);
+    }
+    k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
+    if (n > 0) {
+        k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
+        k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted);
+        k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, x, y, z, q, type, c->d_pos[buf],
+                                                           c->d_type[buf], c->d_id[buf], c->d_F64,
+                                                           c->d_F32, c->d_cnt);
+    }
+    MDRL_CUDA(cudaGetLastError());
+    return MDRL_OK;
+}
+
+static mdrl_status check_device_errors(mdrl_ctx *c) {
+    unsigned err = 0;
+    MDRL_CUDA(cudaMemcpy(&err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (err & kErrPosition) {
+        set_error("positions must be finite and lie in [0, box) on every axis");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    return MDRL_OK;
+}
+
+static mdrl_status read_stats(mdrl_ctx *c, mdrl_stats *st, float ms) {
+    if (!st) return MDRL_OK;
+    DevTotals t;
+    MDRL_CUDA(cudaMemcpy(&t, c->d_tot, sizeof(t), cudaMemcpyDeviceToHost));
+    memset(st, 0, sizeof(*st));
+    st->pairs = (int64_t)t.pairs;
+    st->below_table = (int64_t)t.below;
+    st->max_cell_occupancy = t.max_occ;
+    st->ncells = c->ncells;
+    st->e_lj = t.e_lj;
+    st->e_coul = t.e_coul;
+    st->virial = t.virial;
+    st->kinetic = t.kinetic;
+    st->device_ms = ms;
+    st->pairs_total = (int64_t)t.pairs_total;
+    float fms = 0.0f;
+    if (cudaEventElapsedTime(&fms, c->evf0, c->evf1) == cudaSuccess) st->force_ms = fms;
+    else cudaGetLastError();
+    return MDRL_OK;
+}
+
+static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                  const float *q, const int *type, float *fx, float *fy, float *fz,
+                                  int *counts, mdrl_stats *st) {
+    MDRL_TRY(ensure_capacity(c, n));
+    const bool extra = counts != nullptr || (c->p.flags & MDRL_FLAG_ENERGY);
+    MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
+    MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
+    MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0));
+    MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
+    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, 0, c->d_kepart, c->d_tot);
+    if (n > 0)
+        k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, c->d_F32, c->d_cnt, fx, fy,
+                                                      fz, counts);
+    MDRL_CUDA(cudaGetLastError());
+    MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0.0f;
+    MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    MDRL_TRY(check_device_errors(c));
+    MDRL_TRY(read_stats(c, st, ms));
+    if (st) st->candidates = -1;
+    c->have_state = false; /* the sorted buffers now hold this evaluation */
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_force_eval_device(mdrl_ctx *c, int n, const float *x, const float *y,
+                                              const float *z, const float *q, const int *type,
+                                              float *fx, float *fy, float *fz, int *counts,
+                                              mdrl_stats *st) {
+    if (!c || n < 0 || (n > 0 && (!x || !y || !z || !fx || !fy || !fz))) {
+        set_error("mdrl_force_eval_device: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    return force_eval_dev(c, n, x, y, z, q, type, fx, fy, fz, counts, st);
+}
+
+extern "C" mdrl_status mdrl_force_eval(mdrl_ctx *c, int n, const float *x, const float *y,
+                                       const float *z, const float *q, const int *type, float *fx,
+                                       float *fy, float *fz, int *counts, mdrl_stats *st) {
+    if (!c || n < 0 || (n > 0 && (!x || !y || !z || !fx || !fy || !fz))) {
+        set_error("mdrl_force_eval: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    MDRL_TRY(ensure_capacity(c, n));
+    const size_t fb = sizeof(float) * (size_t)n;
+    if (n > 0) {
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uz, z, fb, cudaMemcpyHostToDevice, c->stream));
+        if (q) MDRL_CUDA(cudaMemcpyAsync(c->d_uq, q, fb, cudaMemcpyHostToDevice, c->stream));
+        if (type) MDRL_CUDA(cudaMemcpyAsync(c->d_ut, type, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    }
+    MDRL_TRY(force_eval_dev(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr,
+                            type ? c->d_ut : nullptr, c->d_ox, c->d_oy, c->d_oz,
+                            counts ? c->d_ocnt : nullptr, st));
+    if (n > 0) {
+        MDRL_CUDA(cudaMemcpyAsync(fx, c->d_ox, fb, cudaMemcpyDeviceToHost, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(fy, c->d_oy, fb, cudaMemcpyDeviceToHost, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(fz, c->d_oz, fb, cudaMemcpyDeviceToHost, c->stream));
+        if (counts) MDRL_CUDA(cudaMemcpyAsync(counts, c->d_ocnt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_bin(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                int *cell_of, int *cell_count, int *order) {
+    if (!c || n < 0 || (n > 0 && (!x || !y || !z))) {
+        set_error("mdrl_bin: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    MDRL_TRY(ensure_capacity(c, n));
+    const size_t fb = sizeof(float) * (size_t)n;
+    if (n > 0) {
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uz, z, fb, cudaMemcpyHostToDevice, c->stream));
+    }
+    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, nullptr, nullptr, 0));
+    if (cell_of && n > 0) MDRL_CUDA(cudaMemcpyAsync(cell_of, c->d_cell_of, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (cell_count) MDRL_CUDA(cudaMemcpyAsync(cell_count, c->d_count, sizeof(int) * c->ncells, cudaMemcpyDeviceToHost, c->stream));
+    if (order && n > 0) MDRL_CUDA(cudaMemcpyAsync(order, c->d_sorted, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    MDRL_TRY(check_device_errors(c));
+    c->have_state = false;
+    return MDRL_OK;
+}
+
+/* ---- tables ------------------------------------------------------------------------------- */
+
+extern "C" mdrl_status mdrl_set_tables(mdrl_ctx *c, int order, int nseg, int bins, int min_log2,
+                                       int nfunc, const float *coef, int raw) {
+    if (!c || !coef || order < 1 || order > 3 || nseg < 1 || bins < 16 || bins > 4096 ||
+        (bins & (bins - 1)) || (nfunc != 2 && nfunc != 3 && nfunc != 6)) {
+        set_error("mdrl_set_tables: invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    const double top = std::ldexp(1.0, min_log2 + nseg);
+    if (!((double)c->g.rc2 < top)) {
+        set_error("mdrl_set_tables: the tables end below rc^2");
+        return MDRL_ERR_RANGE;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    const int nidx = nseg * bins, nc = order + 1;
+    c->order = order; c->nseg = nseg; c->bins = bins; c->min_log2 = min_log2;
+    c->raw = raw != 0;
+    c->tab.assign((size_t)kNumFunc * nc * nidx, 0.0f);
+    memcpy(c->tab.data(), coef, sizeof(float) * (size_t)nfunc * nc * nidx);
+    for (int k = 0; k < 2; ++k) {
+        if (c->graph_exec[k]) { cudaGraphExecDestroy(c->graph_exec[k]); c->graph_exec[k] = nullptr; }
+        if (c->graph[k]) { cudaGraphDestroy(c->graph[k]); c->graph[k] = nullptr; }
+    }
+    c->graph_n = -1;
+    return upload_tables(c);
+}
+
+extern "C" mdrl_status mdrl_get_tables(mdrl_ctx *c, int *order, int *nseg, int *bins, int *min_log2,
+                                       float *coef) {
+    if (!c) { set_error("null context"); return MDRL_ERR_INVALID_ARG; }
+    if (order) *order = c->order;
+    if (nseg) *nseg = c->nseg;
+    if (bins) *bins = c->bins;
+    if (min_log2) *min_log2 = c->min_log2;
+    if (coef) memcpy(coef, c->tab.data(), sizeof(float) * c->tab.size());
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_get_pair_coefficients(mdrl_ctx *c, float *coef) {
+    if (!c || !coef) { set_error("null argument"); return MDRL_ERR_INVALID_ARG; }
+    const int T = c->p.ntypes;
+    for (int k = 0; k < T * T; ++k) {
+        if (c->raw) { coef[4 * k] = 1.0f; coef[4 * k + 1] = -1.0f; coef[4 * k + 2] = 1.0f; coef[4 * k + 3] = -1.0f; }
+        else memcpy(coef + 4 * k, c->pcoef.data() + 4 * k, sizeof(float) * 4);
+    }
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples,
+                                       float *coef) {
+    if (!coef || order < 1 || order > 3 || nseg < 1 || bins < 1 || samples < order + 1 || samples > 1024) {
+        set_error("mdrl_fit_tables: invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    std::vector<float> t;
+    fit_tables(order, nseg, bins, min_log2, samples, &t);
+    memcpy(coef, t.data(), sizeof(float) * t.size());
+    return MDRL_OK;
+}
+
+/* ---- per-pair plugin ---------------------------------------------------------------------- */
+
+typedef void (*pair_fn)(int, const float4 *, const float4 *, const int *, const int *, Geom, TableDev,
+                        const float4 *, int, float, float4 *, float2 *);
+
+static pair_fn pick_pair(int order, bool sep) {
+    switch (order) {
+        case 0: return sep ? (pair_fn)k_pair_eval<0, true> : (pair_fn)k_pair_eval<0, false>;
+        case 1: return sep ? (pair_fn)k_pair_eval<1, true> : (pair_fn)k_pair_eval<1, false>;
+        case 2: return sep ? (pair_fn)k_pair_eval<2, true> : (pair_fn)k_pair_eval<2, false>;
+        default: return sep ? (pair_fn)k_pair_eval<3, true> : (pair_fn)k_pair_eval<3, false>;
+    }
+}
+
+extern "C" mdrl_status mdrl_pair_eval(mdrl_ctx *c, int n, const float *ref, const float *nbr,
+                                      const int *tref, const int *tnbr, float *out, float *aux) {
+    if (!c || n < 0 || (n > 0 && (!ref || !nbr || !out))) {
+        set_error("mdrl_pair_eval: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (n == 0) return MDRL_OK;
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    if (n > c->pcap) {
+        MDRL_TRY(dalloc(&c->d_pr, n)); MDRL_TRY(dalloc(&c->d_pn, n)); MDRL_TRY(dalloc(&c->d_pout, n));
+        MDRL_TRY(dalloc(&c->d_ptr, n)); MDRL_TRY(dalloc(&c->d_ptn, n)); MDRL_TRY(dalloc(&c->d_paux, n));
+        c->pcap = n;
+    }
+    MDRL_CUDA(cudaMemcpyAsync(c->d_pr, ref, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+    MDRL_CUDA(cudaMemcpyAsync(c->d_pn, nbr, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+    if (tref) MDRL_CUDA(cudaMemcpyAsync(c->d_ptr, tref, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    if (tnbr) MDRL_CUDA(cudaMemcpyAsync(c->d_ptn, tnbr, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    Geom g = c->g;
+    if (c->p.flags & MDRL_FLAG_NO_PBC)
+        for (int d = 0; d < 3; ++d) { g.L[d] = 0.0f; g.h[d] = 0.0f; }
+    pair_fn fn = pick_pair(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE);
+    fn<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pr, c->d_pn, tref ? c->d_ptr : nullptr,
+                                            tnbr ? c->d_ptn : nullptr, g, table_dev(c), c->d_pcoef,
+                                            c->p.ntypes, c->ke, c->d_pout, aux ? c->d_paux : nullptr);
+    MDRL_CUDA(cudaGetLastError());
+    MDRL_CUDA(cudaMemcpyAsync(out, c->d_pout, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (aux) MDRL_CUDA(cudaMemcpyAsync(aux, c->d_paux, sizeof(float2) * n, cudaMemcpyDeviceToHost, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    return MDRL_OK;
+}
+
+/* ---- molecular dynamics on device state ---------------------------------------------------- */
+
+extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                      const float *vx, const float *vy, const float *vz, const float *q,
+                                      const int *type) {
+    if (!c || n <= 0 || !x || !y || !z || ((vx || vy || vz) && !(vx && vy && vz))) {
+        set_error("mdrl_set_state: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    MDRL_TRY(ensure_capacity(c, n));
+    const size_t fb = sizeof(float) * (size_t)n;
+    MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));
+    MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
+    MDRL_CUDA(cudaMemcpyAsync(c->d_uz, z, fb, cudaMemcpyHostToDevice, c->stream));
+    if (q) MDRL_CUDA(cudaMemcpyAsync(c->d_uq, q, fb, cudaMemcpyHostToDevice, c->stream));
+    if (type) MDRL_CUDA(cudaMemcpyAsync(c->d_ut, type, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    if (vx) {
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ovx, vx, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ovy, vy, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ovz, vz, fb, cudaMemcpyHostToDevice, c->stream));
+    }
+    if (type) {
+        std::vector<int> chk(type, type + n);
+        for (int i = 0; i < n; ++i)
+            if (chk[i] < 0 || chk[i] >= c->p.ntypes) { set_error("particle type out of range"); return MDRL_ERR_INVALID_ARG; }
+    }
+    MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
+    c->cur = 0;
+    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0));
+    k_gather_vel<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], vx ? c->d_ovx : nullptr, c->d_ovy,
+                                                      c->d_ovz, c->d_vel[0]);
+    const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
+    MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
+    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->mt_half, 0,
+                                                c->d_kepart);
+    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot);
+    MDRL_CUDA(cudaGetLastError());
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    MDRL_TRY(check_device_errors(c));
+    c->n = n;
+    c->have_state = true;
+    return MDRL_OK;
+}
+
+/* One step of kernels on the context stream (captured into a graph by mdrl_step). */
+static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
+    const int n = c->n;
+    const int a = c->cur, b = 1 - c->cur;
+    const bool vv = c->p.integrator == MDRL_INT_VELOCITY_VERLET;
+    const MassTab &mt = vv ? c->mt_half : c->mt_full;
+    const float dt = (float)c->p.dt_fs;
+    MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
+    k_kick_drift_bin<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pos[a], c->d_vel[a], c->d_type[a], c->d_F64,
+                                                          c->d_F32, mt, dt, c->g, c->d_cell_of, c->d_slot,
+                                                          c->d_count);
+    k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
+    k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
+    k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted);
+    k_gather_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, c->d_pos[a], c->d_vel[a], c->d_type[a],
+                                                        c->d_id[a], c->d_pos[b], c->d_vel[b], c->d_type[b],
+                                                        c->d_id[b], c->d_F64, c->d_F32);
+    if (extra) MDRL_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * (size_t)n, c->stream));
+    MDRL_TRY(launch_force(c, n, c->d_pos[b], c->d_type[b], extra));
+    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->mt_half,
+                                                vv ? 1 : 0, c->d_kepart);
+    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, nblk(n, 256), c->d_kepart,
+                                       c->d_tot);
+    MDRL_CUDA(cudaGetLastError());
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_step(mdrl_ctx *c, int nsteps, mdrl_stats *st) {
+    if (!c || nsteps < 0) { set_error("mdrl_step: invalid argument"); return MDRL_ERR_INVALID_ARG; }
+    if (!c->have_state) { set_error("mdrl_step: call mdrl_set_state first"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
+    MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, offsetof(DevTotals, pairs_total), c->stream));
+    MDRL_CUDA(cudaMemsetAsync(&c->d_tot->pairs_total, 0, sizeof(unsigned long long), c->stream));
+    if (c->graph_n != c->n || c->graph_extra != extra) {
+        /* Capture one step per buffer parity (slot 0 -> 1 and slot 1 -> 0). */
+        const int saved = c->cur;
+        for (int k = 0; k < 2; ++k) {
+            if (c->graph_exec[k]) { cudaGraphExecDestroy(c->graph_exec[k]); c->graph_exec[k] = nullptr; }
+            if (c->graph[k]) { cudaGraphDestroy(c->graph[k]); c->graph[k] = nullptr; }
+            c->cur = k;
+            MDRL_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            const mdrl_status s = enqueue_step(c, extra);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            c->cur = saved;
+            if (s != MDRL_OK) { if (g) cudaGraphDestroy(g); return s; }
+            if (e != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(e)); return MDRL_ERR_CUDA; }
+            c->graph[k] = g;
+            MDRL_CUDA(cudaGraphInstantiate(&c->graph_exec[k], g, 0));
+        }
+        c->graph_n = c->n;
+        c->graph_extra = extra;
+    }
+    MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int k = 0; k < nsteps; ++k) {
+        MDRL_CUDA(cudaGraphLaunch(c->graph_exec[c->cur], c->stream));
+        c->cur ^= 1;
+    }
+    MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0.0f;
+    MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    return read_stats(c, st, ms);
+}
+
+extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z, float *vx, float *vy,
+                                      float *vz, float *fx, float *fy, float *fz) {
+    if (!c) { set_error("null context"); return MDRL_ERR_INVALID_ARG; }
+    if (!c->have_state) { set_error("mdrl_get_state: no state"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    const int n = c->n, a = c->cur;
+    k_unsort_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[a], c->d_pos[a], c->d_vel[a], c->d_ux, c->d_uy,
+                                                        c->d_uz, c->d_ovx, c->d_ovy, c->d_ovz);
+    k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[a], c->d_F64, c->d_F32, c->d_cnt, c->d_ox, c->d_oy,
+                                                  c->d_oz, nullptr);
+    MDRL_CUDA(cudaGetLastError());
+    const size_t fb = sizeof(float) * (size_t)n;
+    float *dst[9] = {x, y, z, vx, vy, vz, fx, fy, fz};
+    const float *src[9] = {c->d_ux, c->d_uy, c->d_uz, c->d_ovx, c->d_ovy, c->d_ovz, c->d_ox, c->d_oy, c->d_oz};
+    for (int k = 0; k < 9; ++k)
+        if (dst[k]) MDRL_CUDA(cudaMemcpyAsync(dst[k], src[k], fb, cudaMemcpyDeviceToHost, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    return MDRL_OK;
+}

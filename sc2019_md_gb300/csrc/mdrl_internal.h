@@ -1,0 +1,60 @@
+/*
+ * mdrl_internal.h — declarations shared by the libmdrl translation units.
+ */
+#ifndef MDRL_INTERNAL_H
+#define MDRL_INTERNAL_H
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mdrl.h"
+
+namespace mdrl {
+
+/* Table functions, in the order of the canonical coefficient planes. */
+enum { kF14 = 0, kF8 = 1, kF3 = 2, kF12 = 3, kF6 = 4, kF1 = 5, kNumFunc = 6 };
+
+/* Force CTA geometry: 8 warps; a warp evaluates a 32 x 32 (i, j) piece as 8 rows x 4 columns
+ * of lanes, each lane holding 4 i particles. */
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kChunk = 256;       /* particles of one cell staged in shared memory at a time */
+constexpr int kHalfShellCells = 14;
+
+/* Fixed-point force scale: 2^24 units per kcal/mol/Angstrom. */
+constexpr float kFixScale = 16777216.0f;
+constexpr float kFixInv = 5.9604644775390625e-8f;
+
+/* Periodic geometry passed by value to kernels. */
+struct Geom {
+    float L[3];      /* box edges (0 = no wrap) */
+    float h[3];      /* L / 2 */
+    float edge[3];   /* cell edges */
+    int nc[3];       /* cells per dimension */
+    float rc2;
+};
+
+/* Per-unit reduction slots written by the force kernel (one unit = home cell x neighbour). */
+struct UnitOut {
+    double e_lj, e_coul, virial;
+    unsigned long long pairs, below;
+};
+
+/* Device-side totals. */
+struct DevTotals {
+    double e_lj, e_coul, virial, kinetic;
+    unsigned long long pairs, below, pairs_total;
+    int max_occ;
+    int pad;
+};
+
+void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out);
+void mix_pair_coefficients(const mdrl_params &p, std::vector<float> *pc, std::vector<double> *pc64);
+
+void set_error(const std::string &msg);
+
+}  // namespace mdrl
+
+#endif

@@ -1,0 +1,726 @@
+/*
+ * mdrl_kernels.cuh — sm_103a kernels of the range-limited force path.
+ *
+ * Data layout in HBM (all particle arrays are in cell-sorted order after binning):
+ *   pos   float4[n]  (x, y, z, q)        one 16-byte coalesced load per particle
+ *   type  int[n]
+ *   F     3 x int64[n] (SoA, 2^-24 kcal/mol/A fixed point) or 3 x float[n] (FP32-atomic mode)
+ *   cell_start int[ncells + 1]           cell c holds sorted particles [start[c], start[c+1])
+ *
+ * Pair datapath, per candidate (the reference RTL order, SC/r2_compute_with_pbc.v:81-127,
+ * SC/Filter_Logic.v:234, SC/RL_LJ_Evaluate_Pairs_1st_Order.v:179-193,409-468,
+ * SC/RL_Evaluate_Pairs_1st_Order.v:325-395):
+ *   d = x_ref - x_nbr, one conditional +-L wrap per axis;
+ *   r2 = (dx*dx + dy*dy) + dz*dz, each operation rounded (the pair list is bit-identical to an
+ *        all-pairs FP32 evaluation of the same positions);
+ *   keep when 0 < r2 <= rc2;
+ *   table index = (exponent(r2) - 127 - min_log2) * bins + top mantissa bits;
+ *   v_k = c1*r2 + c0 (or Horner for orders 2-3), fscal = ((QQ*v3) + B*v8) + A*v14,
+ *   f = fscal * d, added to i and subtracted from j (Newton's third law).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mdrl_internal.h"
+
+namespace mdrl {
+
+/* Tables packed for the kernels: for order 1, per table index three float2 {c0, c1} (force:
+ * r^-14, r^-8, r^-3; energy: r^-12, r^-6, r^-1); for orders 2-3, three float4 {c0..c3}. */
+struct TableDev {
+    const float2 *f2, *e2;
+    const float4 *f4, *e4;
+    int order, nseg, bins, lb, min_log2;
+    float r2min;
+};
+
+/* The 14 cells of the half shell in the reference's filter order (see oracle/oracle.cpp). */
+__constant__ int c_halfshell[kHalfShellCells][3] = {
+    {0, 0, 0},  {0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 1},  {1, -1, -1}, {1, -1, 0},
+    {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},  {1, 1, -1}, {1, 1, 0},   {1, 1, 1}};
+
+/* Error bits raised by kernels and read by the host after a call. */
+enum : unsigned { kErrPosition = 1u };
+
+struct MassTab {
+    float cm[MDRL_MAX_TYPES];   /* velocity increment per unit force for the kick */
+    float mass[MDRL_MAX_TYPES]; /* amu, for the kinetic energy */
+};
+
+__device__ __forceinline__ float wrap_d(float d, float L, float h) {
+    return d > h ? __fsub_rn(d, L) : (d < -h ? __fadd_rn(d, L) : d);
+}
+
+template <bool SEP>
+__device__ __forceinline__ float madd(float a, float b, float c) {
+    return SEP ? __fadd_rn(__fmul_rn(a, b), c) : __fmaf_rn(a, b, c);
+}
+
+__device__ __forceinline__ int table_index(const TableDev &t, float r2, float &r2e, int &below) {
+    const unsigned b = __float_as_uint(r2);
+    int seg = (int)(b >> 23) - 127 - t.min_log2;
+    int bin = (int)((b >> (23 - t.lb)) & (unsigned)(t.bins - 1));
+    r2e = r2;
+    below = 0;
+    if (seg < 0) {
+        seg = 0; bin = 0; r2e = t.r2min; below = 1;
+    } else if (seg >= t.nseg) {
+        seg = t.nseg - 1; bin = t.bins - 1;
+    }
+    return seg * t.bins + bin;
+}
+
+template <int ORDER, bool SEP>
+__device__ __forceinline__ float poly4(float4 c, float x) {
+    float v = (ORDER >= 3) ? c.w : c.z;
+    if (ORDER >= 3) v = madd<SEP>(v, x, c.z);
+    v = madd<SEP>(v, x, c.y);
+    return madd<SEP>(v, x, c.x);
+}
+
+/* The pair functions v14, v8, v3 (and v12, v6, v1 when ENERGY) at r2. */
+template <int ORDER, bool SEP, bool ENERGY>
+__device__ __forceinline__ void pair_functions(const TableDev &t, float r2, bool coul, float &v14,
+                                               float &v8, float &v3, float &v12, float &v6,
+                                               float &v1, int &below) {
+    if (ORDER == 0) {
+        const float i2 = __fdiv_rn(1.0f, r2);
+        const float i4 = __fmul_rn(i2, i2), i6 = __fmul_rn(i4, i2), i8 = __fmul_rn(i4, i4);
+        const float i12 = __fmul_rn(i6, i6), i14 = __fmul_rn(i12, i2);
+        const float i1 = __fsqrt_rn(i2), i3 = __fmul_rn(i2, i1);
+        v14 = i14; v8 = i8; v3 = i3; v12 = i12; v6 = i6; v1 = i1;
+        below = 0;
+        return;
+    }
+    float r2e;
+    const int idx = table_index(t, r2, r2e, below);
+    if (ORDER == 1) {
+        const float2 a = __ldg(t.f2 + 3 * idx), b = __ldg(t.f2 + 3 * idx + 1);
+        v14 = madd<SEP>(a.y, r2e, a.x);
+        v8 = madd<SEP>(b.y, r2e, b.x);
+        v3 = 0.0f;
+        if (coul) { const float2 c = __ldg(t.f2 + 3 * idx + 2); v3 = madd<SEP>(c.y, r2e, c.x); }
+        if (ENERGY) {
+            const float2 d = __ldg(t.e2 + 3 * idx), e = __ldg(t.e2 + 3 * idx + 1);
+            v12 = madd<SEP>(d.y, r2e, d.x);
+            v6 = madd<SEP>(e.y, r2e, e.x);
+            v1 = 0.0f;
+            if (coul) { const float2 g = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(g.y, r2e, g.x); }
+        }
+    } else {
+        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), r2e);
+        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), r2e);
+        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), r2e) : 0.0f;
+        if (ENERGY) {
+            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), r2e);
+            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), r2e);
+            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), r2e) : 0.0f;
+        }
+    }
+}
+
+/* fscal = ((QQ*v3) + B*v8) + A*v14 ; energies el = Be*v6 + Ae*v12, ec = QQ*v1. */
+template <bool SEP>
+__device__ __forceinline__ float combine_force(float4 pc, float qq, bool coul, float v14, float v8,
+                                               float v3) {
+    if (SEP) {
+        float fs = __fmul_rn(pc.y, v8);
+        if (coul) fs = __fadd_rn(__fmul_rn(qq, v3), fs);
+        return __fadd_rn(fs, __fmul_rn(pc.x, v14));
+    }
+    const float fs = __fmaf_rn(pc.y, v8, coul ? __fmul_rn(qq, v3) : 0.0f);
+    return __fmaf_rn(pc.x, v14, fs);
+}
+
+template <bool SEP>
+__device__ __forceinline__ float combine_elj(float4 pc, float v12, float v6) {
+    return SEP ? __fadd_rn(__fmul_rn(pc.w, v6), __fmul_rn(pc.z, v12))
+               : __fmaf_rn(pc.z, v12, __fmul_rn(pc.w, v6));
+}
+
+__device__ __forceinline__ unsigned long long to_fixed(float v) {
+    float s = v * kFixScale;
+    if (!(s == s)) s = 0.0f;
+    s = fminf(fmaxf(s, -9.0e18f), 9.0e18f);
+    return (unsigned long long)__float2ll_rn(s);
+}
+
+__device__ __forceinline__ float from_fixed(unsigned long long v) {
+    return __ll2float_rn((long long)v) * kFixInv;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Binning: cell = floor(pos / edge) (MS/GenInputCellList_LJArgon.m:98-112), stable within the
+ * cell (input order, :114-121).  count -> scan -> scatter -> per-cell rank sort.              */
+
+__device__ __forceinline__ int cell_coord(float v, float edge, int n) {
+    const float f = floorf(__fdiv_rn(v, edge));
+    if (!(f >= 0.0f)) return 0;
+    if (f >= (float)n) return n - 1;
+    return (int)f;
+}
+
+__device__ __forceinline__ int cell_of_pos(const Geom &g, float x, float y, float z) {
+    const int cx = cell_coord(x, g.edge[0], g.nc[0]);
+    const int cy = cell_coord(y, g.edge[1], g.nc[1]);
+    const int cz = cell_coord(z, g.edge[2], g.nc[2]);
+    return (cx * g.nc[1] + cy) * g.nc[2] + cz;
+}
+
+__device__ __forceinline__ bool in_box(const Geom &g, float x, float y, float z) {
+    return x >= 0.0f && x < g.L[0] && y >= 0.0f && y < g.L[1] && z >= 0.0f && z < g.L[2];
+}
+
+/* Cell of each user-order particle, with its arrival slot in the cell. */
+__global__ void k_bin_user(int n, const float *__restrict__ x, const float *__restrict__ y,
+                           const float *__restrict__ z, Geom g, int *__restrict__ cell_of,
+                           int *__restrict__ slot, int *__restrict__ count,
+                           unsigned *__restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float px = x[i], py = y[i], pz = z[i];
+    if (!in_box(g, px, py, pz)) atomicOr(err, kErrPosition);
+    const int c = cell_of_pos(g, px, py, pz);
+    cell_of[i] = c;
+    slot[i] = atomicAdd(count + c, 1);
+}
+
+/* Exclusive scan of the cell counts (one CTA), plus the largest occupancy. */
+__global__ void __launch_bounds__(1024) k_scan(int ncells, const int *__restrict__ count,
+                                               int *__restrict__ start, DevTotals *tot) {
+    __shared__ int s_sum[1024];
+    __shared__ int s_max[1024];
+    const int t = threadIdx.x;
+    const int per = (ncells + 1023) / 1024;
+    const int b = t * per, e = min(ncells, b + per);
+    int sum = 0, mx = 0;
+    for (int k = b; k < e; ++k) { const int c = count[k]; sum += c; mx = max(mx, c); }
+    s_sum[t] = sum;
+    s_max[t] = mx;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int v = (t >= off) ? s_sum[t - off] : 0;
+        const int m = (t >= off) ? s_max[t - off] : 0;
+        __syncthreads();
+        s_sum[t] += v;
+        s_max[t] = max(s_max[t], m);
+        __syncthreads();
+    }
+    int run = s_sum[t] - sum;
+    for (int k = b; k < e; ++k) { start[k] = run; run += count[k]; }
+    if (t == 1023) { start[ncells] = s_sum[1023]; tot->max_occ = s_max[1023]; }
+}
+
+__global__ void k_scatter(int n, const int *__restrict__ cell_of, const int *__restrict__ slot,
+                          const int *__restrict__ start, int *__restrict__ tmp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    tmp[start[cell_of[i]] + slot[i]] = i;
+}
+
+/* Order each cell's ids ascending: the rank of an id is the number of smaller ids in its cell. */
+__global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start,
+                                                   const int *__restrict__ tmp,
+                                                   int *__restrict__ sorted) {
+    __shared__ int s_ids[1024];
+    const int c = blockIdx.x;
+    const int s = start[c], m = start[c + 1] - s;
+    if (m == 0) return;
+    const bool staged = m <= 1024;
+    if (staged) {
+        for (int e = threadIdx.x; e < m; e += blockDim.x) s_ids[e] = tmp[s + e];
+        __syncthreads();
+    }
+    const int *ids = staged ? s_ids : tmp + s;
+    for (int e = threadIdx.x; e < m; e += blockDim.x) {
+        const int id = ids[e];
+        int r = 0;
+        for (int q = 0; q < m; ++q) r += ids[q] < id;
+        sorted[s + r] = id;
+    }
+}
+
+/* Gather user-order inputs into cell order and clear the force accumulators. */
+__global__ void k_gather_user(int n, const int *__restrict__ sorted, const float *__restrict__ x,
+                              const float *__restrict__ y, const float *__restrict__ z,
+                              const float *__restrict__ q, const int *__restrict__ type,
+                              float4 *__restrict__ pos, int *__restrict__ ptype,
+                              int *__restrict__ pid, unsigned long long *__restrict__ F64,
+                              float *__restrict__ F32, int *__restrict__ counts) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = sorted[k];
+    pos[k] = make_float4(x[id], y[id], z[id], q ? q[id] : 0.0f);
+    ptype[k] = type ? type[id] : 0;
+    pid[k] = id;
+    if (F64) { F64[k] = 0ull; F64[n + k] = 0ull; F64[2 * n + k] = 0ull; }
+    if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
+    if (counts) counts[k] = 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Half-shell force.  One CTA per unit (home cell h, half-shell neighbour f): the CTA stages
+ * h's and the neighbour's particles in shared memory (256 at a time) and its 8 warps split the
+ * (i, j) square into 32 x 32 pieces.  In a piece, lane (row, col) holds i = row + 8k (k < 4)
+ * in registers and takes j = 4*step + col; the j force of a step is reduced over the 8 rows
+ * with shuffles and added to the warp's private shared-memory accumulator, the i force is
+ * summed in registers over the piece and reduced over the 4 columns.  At the end of the unit
+ * the 8 warp accumulators are summed in warp order, converted to int64 fixed point and added
+ * to global memory with one atomic per particle and component.  Every FP32 sum has a fixed
+ * order, and the int64 sums are exact, so forces are bit-reproducible run to run.
+ * For the home cell itself (f = 0) only pairs i < j in cell order are taken.                 */
+
+template <int ORDER, bool SEP, bool EXTRA, int ACC>
+__global__ void __launch_bounds__(kThreads, 2)
+k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
+        const int *__restrict__ cstart, Geom g, TableDev tab, const float4 *__restrict__ pcoef,
+        int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
+        float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout) {
+    extern __shared__ float4 smem[];
+    float4 *sIp = smem;
+    float4 *sJp = sIp + kChunk;
+    float4 *sCoef = sJp + kChunk;                                      /* [ntypes^2] */
+    int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
+    int *sJt = sIt + kChunk;
+    float *sFi = reinterpret_cast<float *>(sJt + kChunk);              /* [kWarps][3][kChunk] */
+    float *sFj = sFi + kWarps * 3 * kChunk;
+    int *sCi = reinterpret_cast<int *>(sFj + kWarps * 3 * kChunk);     /* EXTRA: [kWarps][kChunk] */
+    int *sCj = sCi + kWarps * kChunk;
+    __shared__ double s_red[kWarps][3];
+    __shared__ unsigned long long s_cnt[kWarps][2];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int row = lane >> 2, col = lane & 3;
+    const int unit = blockIdx.x;
+    const int h = unit / kHalfShellCells, f = unit - h * kHalfShellCells;
+    const int nyz = g.nc[1] * g.nc[2];
+    const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
+    int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
+    cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
+    cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
+    cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
+    const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
+    const bool self = (f == 0);
+    const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
+    const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
+    const bool coul = ke != 0.0f;
+    const float nan = __int_as_float(0x7fc00000);
+
+    for (int t = tid; t < ntypes * ntypes; t += kThreads) sCoef[t] = pcoef[t];
+
+    float acc_elj = 0.0f, acc_ec = 0.0f, acc_vir = 0.0f;
+    unsigned acc_pairs = 0, acc_below = 0;
+
+    for (int i0 = 0; i0 < ni_all; i0 += kChunk) {
+        for (int j0 = self ? i0 : 0; j0 < nj_all; j0 += kChunk) {
+            const int ni = min(kChunk, ni_all - i0), nj = min(kChunk, nj_all - j0);
+            const bool diag = self && (i0 == j0);
+            __syncthreads();
+            for (int t = tid; t < ni; t += kThreads) {
+                sIp[t] = pos[hs + i0 + t];
+                sIt[t] = ptype[hs + i0 + t] * ntypes;
+            }
+            for (int t = tid; t < nj; t += kThreads) {
+                sJp[t] = pos[cs + j0 + t];
+                sJt[t] = ptype[cs + j0 + t];
+            }
+            for (int t = tid; t < kWarps * 3 * kChunk; t += kThreads) { sFi[t] = 0.0f; sFj[t] = 0.0f; }
+            if (EXTRA)
+                for (int t = tid; t < kWarps * kChunk; t += kThreads) { sCi[t] = 0; sCj[t] = 0; }
+            __syncthreads();
+
+            const int nti = (ni + 31) >> 5, ntj = (nj + 31) >> 5;
+            const int npieces = diag ? nti * (nti + 1) / 2 : nti * ntj;
+            float *wFi = sFi + warp * 3 * kChunk;
+            float *wFj = sFj + warp * 3 * kChunk;
+            int *wCi = sCi + warp * kChunk;
+            int *wCj = sCj + warp * kChunk;
+            for (int p = warp; p < npieces; p += kWarps) {
+                int ti, tj;
+                if (diag) {
+                    int r = p;
+                    ti = 0;
+                    while (r >= nti - ti) { r -= nti - ti; ++ti; }
+                    tj = ti + r;
+                } else {
+                    ti = p / ntj;
+                    tj = p - ti * ntj;
+                }
+                float xi[4], yi[4], zi[4], qi[4];
+                int tti[4], il[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    il[k] = ti * 32 + row + 8 * k;
+                    if (il[k] < ni) {
+                        const float4 pp = sIp[il[k]];
+                        xi[k] = pp.x; yi[k] = pp.y; zi[k] = pp.z;
+                        qi[k] = __fmul_rn(ke, pp.w);
+                        tti[k] = sIt[il[k]];
+                    } else {
+                        xi[k] = nan; yi[k] = nan; zi[k] = nan; qi[k] = 0.0f; tti[k] = 0;
+                    }
+                }
+                float fix[4] = {0.f, 0.f, 0.f, 0.f}, fiy[4] = {0.f, 0.f, 0.f, 0.f},
+                      fiz[4] = {0.f, 0.f, 0.f, 0.f};
+                int ci[4] = {0, 0, 0, 0};
+#pragma unroll 2
+                for (int s = 0; s < 8; ++s) {
+                    const int jl = tj * 32 + s * 4 + col;
+                    float xj = nan, yj = nan, zj = nan, qj = 0.0f;
+                    int ttj = 0;
+                    if (jl < nj) {
+                        const float4 pp = sJp[jl];
+                        xj = pp.x; yj = pp.y; zj = pp.z; qj = pp.w;
+                        ttj = sJt[jl];
+                    }
+                    float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+                    int cj = 0;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float dx = wrap_d(__fsub_rn(xi[k], xj), g.L[0], g.h[0]);
+                        const float dy = wrap_d(__fsub_rn(yi[k], yj), g.L[1], g.h[1]);
+                        const float dz = wrap_d(__fsub_rn(zi[k], zj), g.L[2], g.h[2]);
+                        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                   __fmul_rn(dz, dz));
+                        bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
+                        if (diag) ok = ok && (il[k] < jl);
+                        if (ok) {
+                            float v14, v8, v3, v12, v6, v1;
+                            int below;
+                            pair_functions<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1,
+                                                              below);
+                            const float4 pc = sCoef[tti[k] + ttj];
+                            const float qq = __fmul_rn(qi[k], qj);
+                            const float fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
+                            const float fx = __fmul_rn(fs, dx), fy = __fmul_rn(fs, dy),
+                                        fz = __fmul_rn(fs, dz);
+                            fix[k] += fx; fiy[k] += fy; fiz[k] += fz;
+                            fjx -= fx; fjy -= fy; fjz -= fz;
+                            ++acc_pairs;
+                            if (EXTRA) {
+                                ++ci[k];
+                                ++cj;
+                                acc_below += below;
+                                acc_elj += combine_elj<SEP>(pc, v12, v6);
+                                if (coul) acc_ec += __fmul_rn(qq, v1);
+                                acc_vir += __fmul_rn(fs, r2);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int o = 4; o < 32; o <<= 1) {
+                        fjx += __shfl_xor_sync(0xffffffffu, fjx, o);
+                        fjy += __shfl_xor_sync(0xffffffffu, fjy, o);
+                        fjz += __shfl_xor_sync(0xffffffffu, fjz, o);
+                        if (EXTRA) cj += __shfl_xor_sync(0xffffffffu, cj, o);
+                    }
+                    if (row == 0 && jl < nj) {
+                        wFj[jl] += fjx;
+                        wFj[kChunk + jl] += fjy;
+                        wFj[2 * kChunk + jl] += fjz;
+                        if (EXTRA) wCj[jl] += cj;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+#pragma unroll
+                    for (int o = 1; o < 4; o <<= 1) {
+                        fix[k] += __shfl_xor_sync(0xffffffffu, fix[k], o);
+                        fiy[k] += __shfl_xor_sync(0xffffffffu, fiy[k], o);
+                        fiz[k] += __shfl_xor_sync(0xffffffffu, fiz[k], o);
+                        if (EXTRA) ci[k] += __shfl_xor_sync(0xffffffffu, ci[k], o);
+                    }
+                    if (col == 0 && il[k] < ni) {
+                        wFi[il[k]] += fix[k];
+                        wFi[kChunk + il[k]] += fiy[k];
+                        wFi[2 * kChunk + il[k]] += fiz[k];
+                        if (EXTRA) wCi[il[k]] += ci[k];
+                    }
+                }
+            }
+            __syncthreads();
+            /* Flush: sum the warp accumulators in warp order, then one atomic per component. */
+            for (int t = tid; t < ni; t += kThreads) {
+                float v[3];
+                int cc = 0;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    float sacc = 0.0f;
+                    for (int w = 0; w < kWarps; ++w) {
+                        sacc += sFi[(w * 3 + d) * kChunk + t];
+                        if (diag) sacc += sFj[(w * 3 + d) * kChunk + t];
+                    }
+                    v[d] = sacc;
+                }
+                if (EXTRA)
+                    for (int w = 0; w < kWarps; ++w) cc += sCi[w * kChunk + t] + (diag ? sCj[w * kChunk + t] : 0);
+                const int gi = hs + i0 + t;
+                if (ACC == 1) {
+                    atomicAdd(F32 + gi, v[0]); atomicAdd(F32 + n + gi, v[1]); atomicAdd(F32 + 2 * n + gi, v[2]);
+                } else {
+                    atomicAdd(F64 + gi, to_fixed(v[0]));
+                    atomicAdd(F64 + n + gi, to_fixed(v[1]));
+                    atomicAdd(F64 + 2 * n + gi, to_fixed(v[2]));
+                }
+                if (EXTRA && cc) atomicAdd(counts + gi, cc);
+            }
+            if (!diag) {
+                for (int t = tid; t < nj; t += kThreads) {
+                    float v[3];
+                    int cc = 0;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        float sacc = 0.0f;
+                        for (int w = 0; w < kWarps; ++w) sacc += sFj[(w * 3 + d) * kChunk + t];
+                        v[d] = sacc;
+                    }
+                    if (EXTRA)
+                        for (int w = 0; w < kWarps; ++w) cc += sCj[w * kChunk + t];
+                    const int gj = cs + j0 + t;
+                    if (ACC == 1) {
+                        atomicAdd(F32 + gj, v[0]); atomicAdd(F32 + n + gj, v[1]); atomicAdd(F32 + 2 * n + gj, v[2]);
+                    } else {
+                        atomicAdd(F64 + gj, to_fixed(v[0]));
+                        atomicAdd(F64 + n + gj, to_fixed(v[1]));
+                        atomicAdd(F64 + 2 * n + gj, to_fixed(v[2]));
+                    }
+                    if (EXTRA && cc) atomicAdd(counts + gj, cc);
+                }
+            }
+        }
+    }
+
+    /* Unit totals: lane -> warp (shuffles) -> CTA (warp order) -> one slot per unit. */
+    double e1 = acc_elj, e2 = acc_ec, e3 = acc_vir;
+    unsigned long long c1 = acc_pairs, c2 = acc_below;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        if (EXTRA) {
+            e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+            e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+            e3 += __shfl_xor_sync(0xffffffffu, e3, o);
+            c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        }
+    }
+    if (lane == 0) {
+        s_red[warp][0] = e1; s_red[warp][1] = e2; s_red[warp][2] = e3;
+        s_cnt[warp][0] = c1; s_cnt[warp][1] = c2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        UnitOut u;
+        u.e_lj = u.e_coul = u.virial = 0.0;
+        u.pairs = u.below = 0ull;
+        for (int w = 0; w < kWarps; ++w) {
+            u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
+            u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
+        }
+        uout[unit] = u;
+    }
+}
+
+inline size_t force_smem_bytes(int ntypes) {
+    return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
+           sizeof(float) * 2 * kWarps * 3 * kChunk + sizeof(int) * 2 * kWarps * kChunk;
+}
+
+/* Totals over units and kinetic-energy partials, in a fixed order (one CTA). */
+__global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__restrict__ uout,
+                                                int nke, const double *__restrict__ kepart,
+                                                DevTotals *tot) {
+    __shared__ double s_d[256][4];
+    __shared__ unsigned long long s_u[256][2];
+    const int t = threadIdx.x;
+    double a = 0, b = 0, c = 0, k = 0;
+    unsigned long long p = 0, q = 0;
+    for (int u = t; u < nunits; u += 256) {
+        a += uout[u].e_lj; b += uout[u].e_coul; c += uout[u].virial;
+        p += uout[u].pairs; q += uout[u].below;
+    }
+    for (int u = t; u < nke; u += 256) k += kepart[u];
+    s_d[t][0] = a; s_d[t][1] = b; s_d[t][2] = c; s_d[t][3] = k;
+    s_u[t][0] = p; s_u[t][1] = q;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (t < off) {
+            for (int m = 0; m < 4; ++m) s_d[t][m] += s_d[t + off][m];
+            s_u[t][0] += s_u[t + off][0];
+            s_u[t][1] += s_u[t + off][1];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        tot->e_lj = s_d[0][0]; tot->e_coul = s_d[0][1]; tot->virial = s_d[0][2];
+        if (nke > 0) tot->kinetic = s_d[0][3];
+        tot->pairs = s_u[0][0]; tot->below = s_u[0][1];
+        tot->pairs_total += s_u[0][0];
+    }
+}
+
+/* Sorted forces back to user order as float (and counts). */
+__global__ void k_unsort(int n, const int *__restrict__ pid, const unsigned long long *__restrict__ F64,
+                         const float *__restrict__ F32, const int *__restrict__ cnt_s,
+                         float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ fz,
+                         int *__restrict__ cnt_u) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = pid[k];
+    if (F64) {
+        fx[id] = from_fixed(F64[k]); fy[id] = from_fixed(F64[n + k]); fz[id] = from_fixed(F64[2 * n + k]);
+    } else {
+        fx[id] = F32[k]; fy[id] = F32[n + k]; fz[id] = F32[2 * n + k];
+    }
+    if (cnt_u) cnt_u[id] = cnt_s[k];
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Motion update on cell-sorted state.                                                         */
+
+__device__ __forceinline__ float wrap_pos(float x, float L) {
+    if (x < 0.0f) x = __fadd_rn(x, L);
+    else if (x >= L) x = __fsub_rn(x, L);
+    if (!(x >= 0.0f && x < L)) {
+        x = __fsub_rn(x, __fmul_rn(L, floorf(__fdiv_rn(x, L))));
+        if (!(x >= 0.0f && x < L)) x = 0.0f;
+    }
+    return x;
+}
+
+__device__ __forceinline__ float force_of(const unsigned long long *F64, const float *F32, int n,
+                                          int k, int d) {
+    return F64 ? from_fixed(F64[(size_t)d * n + k]) : F32[(size_t)d * n + k];
+}
+
+/* v += F * cm[type] (half or full kick), x += v * dt, wrap, and bin the new position. */
+__global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                 const int *__restrict__ ptype,
+                                 const unsigned long long *__restrict__ F64,
+                                 const float *__restrict__ F32, MassTab mt, float dt, Geom g,
+                                 int *__restrict__ cell_of, int *__restrict__ slot,
+                                 int *__restrict__ count) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float cm = mt.cm[ptype[k]];
+    float4 v = vel[k];
+    float4 p = pos[k];
+    v.x = __fmaf_rn(force_of(F64, F32, n, k, 0), cm, v.x);
+    v.y = __fmaf_rn(force_of(F64, F32, n, k, 1), cm, v.y);
+    v.z = __fmaf_rn(force_of(F64, F32, n, k, 2), cm, v.z);
+    p.x = wrap_pos(__fmaf_rn(v.x, dt, p.x), g.L[0]);
+    p.y = wrap_pos(__fmaf_rn(v.y, dt, p.y), g.L[1]);
+    p.z = wrap_pos(__fmaf_rn(v.z, dt, p.z), g.L[2]);
+    vel[k] = v;
+    pos[k] = p;
+    const int c = cell_of_pos(g, p.x, p.y, p.z);
+    cell_of[k] = c;
+    slot[k] = atomicAdd(count + c, 1);
+}
+
+/* Reorder the state into the new cell order and clear the force accumulators. */
+__global__ void k_gather_state(int n, const int *__restrict__ sorted,
+                               const float4 *__restrict__ pos0, const float4 *__restrict__ vel0,
+                               const int *__restrict__ type0, const int *__restrict__ id0,
+                               float4 *__restrict__ pos1, float4 *__restrict__ vel1,
+                               int *__restrict__ type1, int *__restrict__ id1,
+                               unsigned long long *__restrict__ F64, float *__restrict__ F32) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int o = sorted[k];
+    pos1[k] = pos0[o];
+    vel1[k] = vel0[o];
+    type1[k] = type0[o];
+    id1[k] = id0[o];
+    if (F64) { F64[k] = 0ull; F64[n + k] = 0ull; F64[2 * n + k] = 0ull; }
+    if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
+}
+
+/* Second half kick (velocity Verlet) and per-block kinetic energy partials. */
+__global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, const int *__restrict__ ptype,
+                                              const unsigned long long *__restrict__ F64,
+                                              const float *__restrict__ F32, MassTab mt, int do_kick,
+                                              double *__restrict__ kepart) {
+    __shared__ double s_k[256];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double ke = 0.0;
+    if (k < n) {
+        const int t = ptype[k];
+        float4 v = vel[k];
+        if (do_kick) {
+            const float cm = mt.cm[t];
+            v.x = __fmaf_rn(force_of(F64, F32, n, k, 0), cm, v.x);
+            v.y = __fmaf_rn(force_of(F64, F32, n, k, 1), cm, v.y);
+            v.z = __fmaf_rn(force_of(F64, F32, n, k, 2), cm, v.z);
+            vel[k] = v;
+        }
+        /* 1/2 m v^2 in kcal/mol with v in A/fs and m in amu: divide by 4.184e-4. */
+        ke = 0.5 * (double)mt.mass[t] *
+             ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z) / 4.184e-4;
+    }
+    s_k[threadIdx.x] = ke;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) s_k[threadIdx.x] += s_k[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) kepart[blockIdx.x] = s_k[0];
+}
+
+/* Sorted state back to user order. */
+__global__ void k_unsort_state(int n, const int *__restrict__ pid, const float4 *__restrict__ pos,
+                               const float4 *__restrict__ vel, float *__restrict__ x,
+                               float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
+                               float *__restrict__ vy, float *__restrict__ vz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = pid[k];
+    const float4 p = pos[k], v = vel[k];
+    x[id] = p.x; y[id] = p.y; z[id] = p.z;
+    vx[id] = v.x; vy[id] = v.y; vz[id] = v.z;
+}
+
+/* Gather user-order velocities into cell order (set_state). */
+__global__ void k_gather_vel(int n, const int *__restrict__ pid, const float *__restrict__ vx,
+                             const float *__restrict__ vy, const float *__restrict__ vz,
+                             float4 *__restrict__ vel) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = pid[k];
+    vel[k] = vx ? make_float4(vx[id], vy[id], vz[id], 0.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Per-pair evaluation: the drop-in for the OpenCL library function RL_LJ_Evaluation.          */
+
+template <int ORDER, bool SEP>
+__global__ void k_pair_eval(int n, const float4 *__restrict__ ref, const float4 *__restrict__ nbr,
+                            const int *__restrict__ tref, const int *__restrict__ tnbr, Geom g,
+                            TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke,
+                            float4 *__restrict__ out, float2 *__restrict__ aux) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 a = ref[k], b = nbr[k];
+    const int ta = tref ? tref[k] : 0, tb = tnbr ? tnbr[k] : 0;
+    const float dx = wrap_d(__fsub_rn(a.x, b.x), g.L[0], g.h[0]);
+    const float dy = wrap_d(__fsub_rn(a.y, b.y), g.L[1], g.h[1]);
+    const float dz = wrap_d(__fsub_rn(a.z, b.z), g.L[2], g.h[2]);
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    float fs = 0.0f;
+    if (r2 > 0.0f && r2 <= g.rc2) {
+        const bool coul = ke != 0.0f;
+        float v14, v8, v3, v12, v6, v1;
+        int below;
+        pair_functions<ORDER, SEP, false>(tab, r2, coul, v14, v8, v3, v12, v6, v1, below);
+        const float4 pc = pcoef[ta * ntypes + tb];
+        const float qq = __fmul_rn(__fmul_rn(ke, a.w), b.w);
+        fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
+        o = make_float4(__fmul_rn(fs, dx), __fmul_rn(fs, dy), __fmul_rn(fs, dz), 0.0f);
+    }
+    out[k] = o;
+    if (aux) aux[k] = make_float2(r2, fs);
+}
+
+}  // namespace mdrl

@@ -1,0 +1,153 @@
+"""Seeded synthetic systems for the workloads of the range-limited force path.
+
+Positions are generated in FP64 and cast to FP32; seeds are 20191117 + workload id (replica r of
+the batched workload adds 1000*r).  Units: Angstrom, kcal/mol, amu, fs, elementary charge.
+
+Workloads (all periodic):
+  lj1728      1,728 argon atoms in a 25.5 A cube, rc 8.5 (3x3x3 cells), LJ only.  A 3.0 A minimum
+              separation at 0.104 /A^3 is geometrically impossible (hard-sphere packing 1.47), so
+              the atoms sit on a 12^3 simple-cubic lattice (2.125 A) with +-0.1 A uniform jitter.
+  ljc92k      92,224 atoms in 108.86 x 108.86 x 77.76 A, rc 12 (9x9x6 cells), 4 LJ types
+              (sigma 2.0-3.8, eps 0.02-0.2, Lorentz-Berthelot), charges +-0.42 e net neutral,
+              uniform placement at 0.1 /A^3 with 1.0 A minimum separation.
+  ljc1m       1,048,576 atoms in a 224 A cube, rc 10 (22^3 cells), 16 types, charges U(-0.8, 0.8)
+              shifted to net zero.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+KCAL_PER_AMU_A2_FS2 = 1.0 / 4.184e-4   # (amu A^2/fs^2) -> kcal/mol
+KB_KCAL = 0.0019872041                   # kcal/(mol K)
+COULOMB_K = 332.0637                     # kcal A / (mol e^2)
+
+
+@dataclasses.dataclass
+class System:
+    name: str
+    box: tuple
+    cutoff: float
+    ncell: tuple
+    pos: np.ndarray          # (n,3) float32 in [0, box)
+    vel: np.ndarray          # (n,3) float32, A/fs
+    q: np.ndarray | None     # (n,) float32 or None
+    type: np.ndarray         # (n,) int32
+    sigma: list
+    epsilon: list
+    mass: list
+    coulomb_k: float
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+    def params(self, **kw):
+        from . import default_params
+        T = len(self.sigma)
+        p = default_params(box=self.box, cutoff=self.cutoff, ncell=self.ncell, ntypes=T,
+                           sigma=self.sigma, epsilon=self.epsilon, mass=self.mass,
+                           coulomb_k=self.coulomb_k)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+def wrap_into_box(pos: np.ndarray, box) -> np.ndarray:
+    """FP32 positions in [0, L) on every axis."""
+    out = np.asarray(pos, dtype=np.float32).copy()
+    for d in range(3):
+        L = np.float32(box[d])
+        c = out[:, d]
+        c[c >= L] -= L
+        c[c < 0] += L
+        c[(c >= L) | (c < 0)] = 0.0
+    return out
+
+
+def maxwell(n: int, mass: np.ndarray, temp: float, rng: np.random.Generator) -> np.ndarray:
+    """Maxwell velocities (A/fs) at temp with the centre-of-mass velocity removed."""
+    sd = np.sqrt(KB_KCAL * temp / mass / KCAL_PER_AMU_A2_FS2)
+    v = rng.standard_normal((n, 3)) * sd[:, None]
+    v -= (mass[:, None] * v).sum(0) / mass.sum()
+    return v.astype(np.float32)
+
+
+def uniform_min_sep(n: int, box, dmin: float, rng: np.random.Generator) -> np.ndarray:
+    """n uniform points in the periodic box with no pair closer than dmin (random sequential
+    re-draws of one member of each violating pair)."""
+    from scipy.spatial import cKDTree
+    box = np.asarray(box, dtype=np.float64)
+    pos = rng.random((n, 3)) * box
+    for _ in range(200):
+        tree = cKDTree(pos, boxsize=box)
+        pairs = tree.query_pairs(dmin, output_type="ndarray")
+        if len(pairs) == 0:
+            return pos
+        bad = np.unique(pairs[:, 1])
+        pos[bad] = rng.random((len(bad), 3)) * box
+    raise RuntimeError("could not place particles with the requested minimum separation")
+
+
+def lj1728(seed_offset: int = 0) -> System:
+    rng = np.random.default_rng(20191117 + 1 + seed_offset)
+    L = 25.5
+    a = L / 12
+    g = (np.arange(12) + 0.5) * a
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    pos += rng.uniform(-0.1, 0.1, pos.shape)
+    pos = wrap_into_box(pos, (L, L, L))
+    m = np.full(len(pos), 39.95)
+    return System("lj1728", (L, L, L), 8.5, (3, 3, 3), pos, maxwell(len(pos), m, 300.0, rng),
+                  None, np.zeros(len(pos), np.int32), [3.4], [0.238], [39.95], 0.0)
+
+
+def ljc92k(n: int = 92224, box=(108.86, 108.86, 77.76), seed_offset: int = 0) -> System:
+    rng = np.random.default_rng(20191117 + 2 + seed_offset)
+    pos = wrap_into_box(uniform_min_sep(n, box, 1.0, rng), box)
+    sigma = [2.0, 2.6, 3.2, 3.8]
+    eps = [0.02, 0.08, 0.14, 0.20]
+    mass = [12.011, 14.007, 15.999, 39.95]
+    t = rng.integers(0, 4, n).astype(np.int32)
+    q = np.full(n, 0.42)
+    q[: n // 2] = -0.42
+    rng.shuffle(q)
+    m = np.asarray(mass)[t]
+    ncell = tuple(int(np.floor(np.float32(b) / np.float32(12.0))) for b in box)
+    return System("ljc92k", tuple(box), 12.0, ncell, pos, maxwell(n, m, 300.0, rng),
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+
+
+def ljc1m(n: int = 1048576, L: float = 224.0, seed_offset: int = 0) -> System:
+    rng = np.random.default_rng(20191117 + 5 + seed_offset)
+    pos = wrap_into_box(rng.random((n, 3)) * L, (L, L, L))
+    T = 16
+    sigma = list(rng.uniform(2.5, 3.8, T))
+    eps = list(rng.uniform(0.05, 0.25, T))
+    mass = list(rng.uniform(12.0, 40.0, T))
+    t = rng.integers(0, T, n).astype(np.int32)
+    q = rng.uniform(-0.8, 0.8, n)
+    q -= q.mean()
+    m = np.asarray(mass)[t]
+    nc = int(np.floor(np.float32(L) / np.float32(10.0)))
+    return System("ljc1m", (L, L, L), 10.0, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+
+
+def small_ljc(n: int, L: float, cutoff: float, seed: int, ntypes: int = 4,
+              dmin: float = 1.0) -> System:
+    """A small LJ+Coulomb system of the ljc92k kind (for parity tests)."""
+    rng = np.random.default_rng(seed)
+    box = (L, L, L)
+    pos = wrap_into_box(uniform_min_sep(n, box, dmin, rng), box)
+    sigma = [2.0, 2.6, 3.2, 3.8][:ntypes]
+    eps = [0.02, 0.08, 0.14, 0.20][:ntypes]
+    mass = [12.011, 14.007, 15.999, 39.95][:ntypes]
+    t = rng.integers(0, ntypes, n).astype(np.int32)
+    q = np.where(rng.random(n) < 0.5, -0.42, 0.42)
+    m = np.asarray(mass)[t]
+    nc = int(np.floor(np.float32(L) / np.float32(cutoff)))
+    return System("small_ljc", box, cutoff, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)

@@ -1,0 +1,192 @@
+"""GPU parity of the range-limited force path against the oracle and the reference's fixtures.
+
+Bit-exact: per-pair r2 / fscal / force components (KAT-1 and random pairs), cell assignment and
+in-cell order (KAT-2), per-particle partner counts and pair totals.  Tolerance-checked: summed
+forces (FP32 partial sums in a fixed order vs the oracle's order-free sum of the same FP32
+per-pair forces: |dF| <= 2e-6 * sum_j |f_ij| per component) and energies (1e-6 relative).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import sc2019_md_gb300 as m
+from sc2019_md_gb300 import systems
+from helpers import force_err, kat1, kat2_positions, oracle_from_ctx
+
+pytestmark = pytest.mark.gpu
+
+SUM_TOL = 2e-6     # |F_gpu - F_oracle| <= SUM_TOL * sum_j |f_ij|, per particle and component
+
+
+def test_pair_eval_kat1_bit_exact():
+    """The 100 x 100 ApoA1 pairs of VERIFICATION_REFERENCE_OUTPUT.txt through mdrl_pair_eval with
+    the reference's ROM tables: r2, F, Fx, Fy, Fz bit-identical for all 10,000 pairs."""
+    pos, expect, tab = kat1()
+    p = m.default_params(box=(1000.0, 1000.0, 1000.0), cutoff=14.0, table_min_log2=-6,
+                         arith=m.ARITH_SEPARATE, flags=m.FLAG_NO_PBC)
+    with m.Context(p) as ctx:
+        ctx.set_tables(tab, order=1, nseg=14, bins=256, min_log2=-6, raw=True)
+        i, j = np.divmod(np.arange(10000), 100)
+        ref = np.concatenate([pos[i], np.zeros((10000, 1), np.float32)], 1)
+        nbr = np.concatenate([pos[j], np.zeros((10000, 1), np.float32)], 1)
+        out, aux = ctx.pair_eval(ref, nbr)
+    got = np.stack([aux[:, 1], out[:, 0], out[:, 1], out[:, 2], aux[:, 0]], 1).view(np.uint32)
+    exp = expect[:, :5]
+    assert np.array_equal(got, exp), f"{int((got != exp).any(1).sum())} of 10000 pairs differ"
+    assert int((exp[:, 0] != 0).sum()) == 9894
+
+
+@pytest.mark.parametrize("order,bins", [(0, 256), (1, 256), (1, 512), (2, 256), (3, 256)])
+@pytest.mark.parametrize("arith", [m.ARITH_FMA, m.ARITH_SEPARATE])
+def test_pair_eval_random_vs_oracle(order, bins, arith):
+    """Random periodic pairs of 4 types with charges: bit-identical to the oracle's datapath."""
+    rng = np.random.default_rng(100 + order * 7 + arith)
+    n = 4000
+    L = 40.0
+    sysm = systems.small_ljc(64, L, 12.0, seed=3)
+    p = sysm.params(table_order=max(order, 1), table_bins=bins, arith=arith,
+                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE)
+    a = rng.uniform(0, L, (n, 3)).astype(np.float32)
+    b = (a + rng.uniform(-13, 13, (n, 3))).astype(np.float32) % np.float32(L)
+    b[:50] = a[:50]                                   # r2 = 0 pairs are filtered
+    qa = rng.choice([-0.42, 0.42], n).astype(np.float32)
+    qb = rng.choice([-0.42, 0.42], n).astype(np.float32)
+    ta = rng.integers(0, 4, n).astype(np.int32)
+    tb = rng.integers(0, 4, n).astype(np.int32)
+    with m.Context(p) as ctx:
+        out, aux = ctx.pair_eval(np.column_stack([a, qa]), np.column_stack([b, qb]), ta, tb)
+        o = oracle_from_ctx(ctx, sysm)
+    exp = np.zeros((n, 5), np.float32)
+    for k in range(n):
+        ok, r = o.pair(a[k], b[k], qa[k], qb[k], ta[k], tb[k])
+        exp[k] = [r[0], r[1], r[2], r[3], r[4]]
+    got = np.column_stack([out[:, :3], aux[:, 1], aux[:, 0]])
+    assert np.array_equal(got.view(np.uint32), exp.view(np.uint32))
+
+
+def test_bin_kat2_bit_exact():
+    """The LJArgon 20k binning (7x6x6 cells of 8.5 A): the 27 cell_ini files' counts, order and
+    FP32 bits, and the whole assignment equal to the oracle's."""
+    pos, d = kat2_positions()
+    p = m.default_params(box=(7 * 8.5, 6 * 8.5, 6 * 8.5), cutoff=8.5, ncell=(7, 6, 6))
+    with m.Context(p) as ctx:
+        cell_of, count, order = ctx.bin(pos[:, 0], pos[:, 1], pos[:, 2])
+    start = np.concatenate([[0], np.cumsum(count)])
+    for cx in range(3):
+        for cy in range(3):
+            for cz in range(3):
+                c = (cx * 6 + cy) * 6 + cz
+                ids = order[start[c]:start[c + 1]]
+                assert len(ids) == d["counts"][cx, cy, cz]
+                assert np.array_equal(pos[ids].view(np.uint32), d[f"c{cx + 1}{cy + 1}{cz + 1}"])
+    oc, ostart, oorder, _ = oracle.bin_cells(pos, p.box, (7, 6, 6))
+    assert np.array_equal(cell_of, oc)
+    assert np.array_equal(order, oorder)
+
+
+def _check_force(sysm, params, tol=SUM_TOL):
+    with m.Context(params) as ctx:
+        x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
+        F, st, cnt = ctx.force(x, y, z, sysm.q, sysm.type, counts=True)
+        F2, st2, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        o = oracle_from_ctx(ctx, sysm)
+    Fo, Fabs, cnto, sto = o.force_cells()
+    assert np.array_equal(cnt, cnto), "partner counts differ"
+    assert st["pairs"] == sto["pairs"]
+    assert st["below_table"] == sto["below_table"]
+    err = np.abs(F - Fo) / np.maximum(Fabs, 1e-30)
+    assert err.max() <= tol, f"max |dF|/sum|f| = {err.max():.3e}"
+    if params.accum == m.ACC_FIXED64:
+        assert np.array_equal(F.view(np.uint32), F2.view(np.uint32)), "not bit-reproducible"
+    for key in ("e_lj", "e_coul", "virial"):
+        ref = sto[key]
+        assert abs(st[key] - ref) <= 1e-5 * max(abs(ref), 1.0), (key, st[key], ref)
+    return F, Fo, o
+
+
+@pytest.mark.parametrize("order,bins", [(0, 256), (1, 256), (1, 512), (2, 256)])
+@pytest.mark.parametrize("arith", [m.ARITH_FMA, m.ARITH_SEPARATE])
+def test_force_small_ljc(order, bins, arith):
+    sysm = systems.small_ljc(3000, 37.5, 12.0, seed=21)          # 3x3x3 cells, ~110 per cell
+    p = sysm.params(table_order=max(order, 1), table_bins=bins, arith=arith,
+                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE, flags=m.FLAG_ENERGY)
+    _check_force(sysm, p)
+
+
+def test_force_lj1728_and_fp64_error():
+    """The 1,728-atom LJ argon cube (3x3x3 cells): parity with the oracle, and the stated force
+    error of 1st-order 512-bin tables against the FP64 direct oracle."""
+    sysm = systems.lj1728()
+    p = sysm.params(table_bins=512, flags=m.FLAG_ENERGY)
+    F, Fo, o = _check_force(sysm, p)
+    F64, _ = o.force_direct64()
+    emax, emed = force_err(F, F64)
+    assert emed <= 1e-5, emed
+    assert emax <= 1e-3, emax
+
+
+def test_force_ljc_fp64_error_512_bins():
+    sysm = systems.small_ljc(6000, 49.6, 12.0, seed=5)
+    p = sysm.params(table_bins=512)
+    with m.Context(p) as ctx:
+        F, st, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
+        o = oracle_from_ctx(ctx, sysm)
+    F64, _ = o.force_direct64()
+    emax, emed = force_err(F, F64)
+    assert emed <= 1e-5, emed
+
+
+def test_force_fp32_atomic_plain():
+    sysm = systems.small_ljc(3000, 37.5, 12.0, seed=22)
+    p = sysm.params(accum=m.ACC_FP32_ATOMIC, table_bins=512)
+    _check_force(sysm, p, tol=1e-5)
+
+
+def test_force_large_cell_chunks():
+    """A cell holding more particles than one shared-memory chunk (256) is processed in chunks."""
+    rng = np.random.default_rng(8)
+    L = 30.0
+    pos = rng.uniform(0, L, (1500, 3)).astype(np.float32)
+    pos[:700] = rng.uniform(0, 10.0, (700, 3)).astype(np.float32)   # > 256 in cell (0,0,0)
+    sysm = systems.System("dense", (L, L, L), 10.0, (3, 3, 3), pos, np.zeros_like(pos), None,
+                          np.zeros(1500, np.int32), [0.5], [0.01], [39.95], 0.0)
+    p = sysm.params(table_min_log2=-8)
+    with m.Context(p) as ctx:
+        F, st, cnt = ctx.force(pos[:, 0], pos[:, 1], pos[:, 2], None, None, counts=True)
+        o = oracle_from_ctx(ctx, sysm)
+    Fo, Fabs, cnto, sto = o.force_cells()
+    assert np.array_equal(cnt, cnto)
+    assert (np.abs(F - Fo) / np.maximum(Fabs, 1e-30)).max() <= SUM_TOL
+
+
+def test_edge_cases():
+    p = m.default_params()
+    with m.Context(p) as ctx:
+        F, st, _ = ctx.force(np.zeros(0), np.zeros(0), np.zeros(0))
+        assert F.shape == (0, 3) and st["pairs"] == 0
+        F, st, _ = ctx.force([1.0], [2.0], [3.0])
+        assert np.all(F == 0) and st["pairs"] == 0
+        # a particle exactly at 0 and one just below L
+        L = np.float32(25.5)
+        x = np.array([0.0, np.nextafter(L, np.float32(0))], np.float32)
+        F, st, _ = ctx.force(x, np.array([1.0, 1.0], np.float32), np.array([1.0, 1.0], np.float32))
+        assert st["pairs"] == 1
+        with pytest.raises(m.MdrlError) as e:
+            ctx.force([26.0], [1.0], [1.0])
+        assert e.value.status == 1
+        with pytest.raises(m.MdrlError):
+            ctx.force([np.nan], [1.0], [1.0])
+    with pytest.raises(m.MdrlError) as e:
+        with m.Context(m.default_params(box=(16.0, 25.5, 25.5))) as ctx:   # 1 cell of 16 A on x
+            ctx.force([1.0], [1.0], [1.0])
+    assert e.value.status == 3
+    with pytest.raises(m.MdrlError):
+        m.Context(m.default_params(table_bins=300))
+
+
+def test_full_size_ljc92k_counts_and_forces():
+    """The 92,224-atom LJ+Coulomb system at full size: partner counts and pair total bit-equal to
+    the oracle, forces within the summation tolerance."""
+    sysm = systems.ljc92k()
+    p = sysm.params(table_bins=512)
+    F, Fo, o = _check_force(sysm, p)
