@@ -188,6 +188,11 @@ mdrl_status mdrl_step(mdrl_ctx *ctx, int nsteps, mdrl_stats *stats);
 mdrl_status mdrl_get_state(mdrl_ctx *ctx, float *x, float *y, float *z, float *vx, float *vy,
                            float *vz, float *fx, float *fy, float *fz);
 
+/* Timing: launch the half-shell force kernel once on the current device state (after
+ * mdrl_set_state / mdrl_step) into a scratch accumulator, bracketed by CUDA events on the
+ * context's stream; *ms receives the kernel's device time.  The state is not modified. */
+mdrl_status mdrl_time_force(mdrl_ctx *ctx, float *ms);
+
 /* Drop-in for the reference C model's entry point.  Reads the argon PDB named by the
  * environment variable MDRL_INPUT (N from MDRL_N, default 500; iterations from MDRL_ITERS,
  * default 100), runs the reference's all-pairs direct FP32 force and symplectic-Euler update on

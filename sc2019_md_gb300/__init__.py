@@ -100,13 +100,14 @@ def lib() -> C.CDLL:
     L.mdrl_set_state.argtypes = [vp, st, _F, _F, _F, _F, _F, _F, _F, _I]
     L.mdrl_step.argtypes = [vp, st, C.POINTER(Stats)]
     L.mdrl_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
+    L.mdrl_time_force.argtypes = [vp, _F]
     L.MD_Evaluation_Model.argtypes = []
     L.MD_Evaluation_Model.restype = C.c_int
     L.mdrl_cmodel_run.argtypes = [st, st, C.c_float, C.c_float, _F, _F, _F, _I]
     for name in ("mdrl_fit_tables", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
                  "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
                  "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
-                 "mdrl_get_state", "mdrl_cmodel_run"):
+                 "mdrl_get_state", "mdrl_cmodel_run", "mdrl_time_force"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -273,6 +274,12 @@ class Context:
         st = Stats()
         _check(lib().mdrl_step(self._h, nsteps, C.byref(st)))
         return st.as_dict()
+
+    def time_force(self) -> float:
+        """Device time (ms) of one launch of the force kernel on the current state."""
+        ms = C.c_float()
+        _check(lib().mdrl_time_force(self._h, C.byref(ms)))
+        return ms.value
 
     def state(self):
         n = self._n

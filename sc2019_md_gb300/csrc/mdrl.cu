@@ -14,7 +14,7 @@
 #include <vector>
 
 #include "mdrl_internal.h"
-#include "mdrl_kernels.cuh"
+#include "mdrl_force.cuh"
 
 using namespace mdrl;
 
@@ -84,6 +84,8 @@ struct mdrl_ctx {
     int *d_count = nullptr, *d_start = nullptr;
     unsigned long long *d_F64 = nullptr;
     float *d_F32 = nullptr;
+    unsigned long long *d_Fscr64 = nullptr; /* scratch accumulators for mdrl_time_force */
+    float *d_Fscr32 = nullptr;
     int *d_cnt = nullptr;
     UnitOut *d_unit = nullptr;
     double *d_kepart = nullptr;
@@ -344,6 +346,7 @@ static void free_particles(mdrl_ctx *c) {
     for (int b = 0; b < 2; ++b) { dfree(&c->d_pos[b]); dfree(&c->d_vel[b]); dfree(&c->d_type[b]); dfree(&c->d_id[b]); }
     dfree(&c->d_cell_of); dfree(&c->d_slot); dfree(&c->d_tmp); dfree(&c->d_sorted);
     dfree(&c->d_F64); dfree(&c->d_F32); dfree(&c->d_cnt);
+    dfree(&c->d_Fscr64); dfree(&c->d_Fscr32);
     c->cap = 0;
 }
 
@@ -409,34 +412,22 @@ static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
 
 /* ---- kernel dispatch ---------------------------------------------------------------------- */
 
-typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
-                         int, float, int, unsigned long long *, float *, int *, UnitOut *);
-
-template <int ORDER, bool SEP, bool EXTRA>
-static force_fn pick_acc(int acc) {
-    return acc == MDRL_ACC_FP32_ATOMIC ? (force_fn)k_force<ORDER, SEP, EXTRA, 1>
-                                       : (force_fn)k_force<ORDER, SEP, EXTRA, 0>;
+namespace mdrl {
+force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap);
+force_fn pick_force_acc1(int order, bool sep, bool extra, bool wrap);
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap) {
+    return acc == MDRL_ACC_FP32_ATOMIC ? pick_force_acc1(order, sep, extra, wrap)
+                                       : pick_force_acc0(order, sep, extra, wrap);
 }
-
-template <int ORDER>
-static force_fn pick_sep(bool sep, bool extra, int acc) {
-    if (sep) return extra ? pick_acc<ORDER, true, true>(acc) : pick_acc<ORDER, true, false>(acc);
-    return extra ? pick_acc<ORDER, false, true>(acc) : pick_acc<ORDER, false, false>(acc);
-}
-
-static force_fn pick_force(int order, bool sep, bool extra, int acc) {
-    switch (order) {
-        case 0: return pick_sep<0>(sep, extra, acc);
-        case 1: return pick_sep<1>(sep, extra, acc);
-        case 2: return pick_sep<2>(sep, extra, acc);
-        default: return pick_sep<3>(sep, extra, acc);
-    }
-}
+}  // namespace mdrl
 
 static int eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
 
-static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra) {
-    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum);
+static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra,
+                                     unsigned long long *F64, float *F32) {
+    /* the per-unit shift needs >= 4 cells on every axis; with 3 the per-pair wrap is used */
+    const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap);
     const size_t smem = force_smem_bytes(c->p.ntypes);
     {
         /* The attribute is set once per kernel and device, outside any stream capture. */
@@ -452,12 +443,15 @@ static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int
     }
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
-    fn<<<units, kThreads, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
-                                              c->p.ntypes, c->ke, n, c->d_F64, c->d_F32, c->d_cnt,
-                                              c->d_unit);
+    fn<<<units, kFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
+                                              c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
+}
+
+static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra) {
+    return launch_force_into(c, n, pos, type, extra, c->d_F64, c->d_F32);
 }
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
@@ -477,7 +471,7 @@ static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, 
         k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted);
         k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, x, y, z, q, type, c->d_pos[buf],
                                                            c->d_type[buf], c->d_id[buf], c->d_F64,
-                                                           c->d_F32, c->d_cnt);
+                                                           c->d_F32, c->d_cnt, c->p.ntypes, c->d_err);
     }
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
@@ -488,6 +482,10 @@ static mdrl_status check_device_errors(mdrl_ctx *c) {
     MDRL_CUDA(cudaMemcpy(&err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (err & kErrPosition) {
         set_error("positions must be finite and lie in [0, box) on every axis");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (err & kErrType) {
+        set_error("particle types must lie in [0, ntypes)");
         return MDRL_ERR_INVALID_ARG;
     }
     return MDRL_OK;
@@ -733,11 +731,6 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
         MDRL_CUDA(cudaMemcpyAsync(c->d_ovy, vy, fb, cudaMemcpyHostToDevice, c->stream));
         MDRL_CUDA(cudaMemcpyAsync(c->d_ovz, vz, fb, cudaMemcpyHostToDevice, c->stream));
     }
-    if (type) {
-        std::vector<int> chk(type, type + n);
-        for (int i = 0; i < n; ++i)
-            if (chk[i] < 0 || chk[i] >= c->p.ntypes) { set_error("particle type out of range"); return MDRL_ERR_INVALID_ARG; }
-    }
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
     c->cur = 0;
     MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0));
@@ -820,6 +813,22 @@ extern "C" mdrl_status mdrl_step(mdrl_ctx *c, int nsteps, mdrl_stats *st) {
     float ms = 0.0f;
     MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     return read_stats(c, st, ms);
+}
+
+extern "C" mdrl_status mdrl_time_force(mdrl_ctx *c, float *ms) {
+    if (!c || !ms) { set_error("mdrl_time_force: null argument"); return MDRL_ERR_INVALID_ARG; }
+    if (!c->have_state) { set_error("mdrl_time_force: call mdrl_set_state first"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    const int n = c->n, a = c->cur;
+    const bool fp32 = c->p.accum == MDRL_ACC_FP32_ATOMIC;
+    if (fp32 && !c->d_Fscr32) MDRL_TRY(dalloc(&c->d_Fscr32, 3 * (size_t)c->cap));
+    if (!fp32 && !c->d_Fscr64) MDRL_TRY(dalloc(&c->d_Fscr64, 3 * (size_t)c->cap));
+    if (fp32) MDRL_CUDA(cudaMemsetAsync(c->d_Fscr32, 0, sizeof(float) * 3 * (size_t)n, c->stream));
+    else MDRL_CUDA(cudaMemsetAsync(c->d_Fscr64, 0, sizeof(unsigned long long) * 3 * (size_t)n, c->stream));
+    MDRL_TRY(launch_force_into(c, n, c->d_pos[a], c->d_type[a], false, c->d_Fscr64, c->d_Fscr32));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    MDRL_CUDA(cudaEventElapsedTime(ms, c->evf0, c->evf1));
+    return MDRL_OK;
 }
 
 extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z, float *vx, float *vy,

@@ -1,0 +1,377 @@
+/*
+ * mdrl_force.cuh — the half-shell pair-force kernel (sm_103a).
+ *
+ * One CTA of 4 warps per unit = (home cell h, half-shell neighbour f), f = 0..13 in the
+ * reference's filter order (SC/Particle_Pair_Gen_HalfShell.v:14-24).  The CTA stages h's and
+ * the neighbour's particles (256 at a time) in shared memory.  The (i, j) square is cut into
+ * pieces of 32 i-particles x (8 * kStepsPerPiece) j-particles, dealt round-robin to the warps.
+ *
+ * Inside a piece, lane = row * 8 + col (4 rows x 8 columns): the lane keeps the 8 i-particles
+ * i = row + 4k (k < 8) in registers, and in each step takes j = 8 * step + col.  A step
+ * evaluates 8 candidates per lane; the j force of the step is summed in registers, reduced over
+ * the 4 rows with two shuffles per component and added to the warp's private shared-memory
+ * accumulator; the i forces stay in registers for the whole piece and are reduce-scattered over
+ * the 8 columns at its end (after which each lane owns one i's complete partial sum).  When the
+ * unit is done the 4 warp accumulators are summed in warp order and added to global memory with
+ * one atomic per particle and component (int64 fixed point 2^-24: exact, so the result does not
+ * depend on the order in which CTAs finish).
+ *
+ * Periodic wrap.  With at least 4 cells of edge >= rc on every axis, whether the reference's
+ * one-wrap rule (d > L/2 -> d - L, d < -L/2 -> d + L; SC/r2_compute_with_pbc.v:81-127) fires
+ * for a pair depends only on whether the neighbour cell lies across the box boundary, so the
+ * unit adds a precomputed -L, 0 or +L to fl(xi - xj): the same two roundings as the per-pair
+ * rule, hence the same r2 bit for bit.  With 3 cells on an axis the per-pair rule is kept
+ * (WRAP = true).
+ *
+ * Table address.  r2e = max(r2, 2^min_log2); (bits(r2e) >> (23 - log2 bins)) - ((127 +
+ * min_log2) << log2 bins) is segment * bins + bin, the address the RTL forms from the exponent
+ * and the top mantissa bits (SC/RL_LJ_Evaluate_Pairs_1st_Order.v:179-193).  Accepted pairs have
+ * r2 <= rc2, and the host guarantees the tables extend past rc2.
+ */
+#pragma once
+
+#include "mdrl_kernels.cuh"
+
+namespace mdrl {
+
+constexpr int kFW = 4;                 /* warps per force CTA */
+constexpr int kFT = kFW * 32;
+constexpr int kStepsPerPiece = 6;      /* j-steps (of 8 particles) per piece */
+
+typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
+                         int, float, int, unsigned long long *, float *, int *, UnitOut *);
+
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap);
+
+inline size_t force_smem_bytes(int ntypes) {
+    return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
+           sizeof(float) * kFW * 6 * kChunk + sizeof(int) * kFW * 2 * kChunk;
+}
+
+template <int ORDER, bool SEP, bool ENERGY>
+__device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2, bool coul,
+                                                    float &v14, float &v8, float &v3, float &v12,
+                                                    float &v6, float &v1) {
+    if (ORDER == 0) {
+        int below;
+        pair_functions<0, SEP, ENERGY>(t, r2, coul, v14, v8, v3, v12, v6, v1, below);
+        return;
+    }
+    const float r2e = fmaxf(r2, t.r2min);
+    const int idx = (int)(__float_as_uint(r2e) >> (23 - t.lb)) - ((127 + t.min_log2) << t.lb);
+    if (ORDER == 1) {
+        const float2 a = __ldg(t.f2 + 3 * idx), b = __ldg(t.f2 + 3 * idx + 1);
+        v14 = madd<SEP>(a.y, r2e, a.x);
+        v8 = madd<SEP>(b.y, r2e, b.x);
+        v3 = 0.0f;
+        if (coul) { const float2 c = __ldg(t.f2 + 3 * idx + 2); v3 = madd<SEP>(c.y, r2e, c.x); }
+        if (ENERGY) {
+            const float2 d = __ldg(t.e2 + 3 * idx), e = __ldg(t.e2 + 3 * idx + 1);
+            v12 = madd<SEP>(d.y, r2e, d.x);
+            v6 = madd<SEP>(e.y, r2e, e.x);
+            v1 = 0.0f;
+            if (coul) { const float2 g = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(g.y, r2e, g.x); }
+        }
+    } else {
+        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), r2e);
+        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), r2e);
+        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), r2e) : 0.0f;
+        if (ENERGY) {
+            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), r2e);
+            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), r2e);
+            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), r2e) : 0.0f;
+        }
+    }
+}
+
+template <bool WRAP>
+__device__ __forceinline__ float pair_diff(float a, float b, float L, float h, float s) {
+    const float d = __fsub_rn(a, b);
+    return WRAP ? wrap_d(d, L, h) : __fadd_rn(d, s);
+}
+
+/* Sum of v over the 8 column lanes, scattered: on return lane col holds, in v[0..2], the sums of
+ * the input v[3*col .. 3*col+2] (each input v has 24 entries). */
+__device__ __forceinline__ void reduce_scatter24(float (&v)[24], int col) {
+    const bool b4 = col & 4, b2 = col & 2, b1 = col & 1;
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+        const float send = b4 ? v[t] : v[12 + t];
+        const float keep = b4 ? v[12 + t] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+        const float send = b2 ? v[t] : v[6 + t];
+        const float keep = b2 ? v[6 + t] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        const float send = b1 ? v[t] : v[3 + t];
+        const float keep = b1 ? v[3 + t] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+    }
+}
+
+__device__ __forceinline__ int reduce_scatter8i(int (&v)[8], int col) {
+    const bool b4 = col & 4, b2 = col & 2, b1 = col & 1;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int send = b4 ? v[t] : v[4 + t];
+        const int keep = b4 ? v[4 + t] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int send = b2 ? v[t] : v[2 + t];
+        const int keep = b2 ? v[2 + t] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    const int send = b1 ? v[0] : v[1];
+    const int keep = b1 ? v[1] : v[0];
+    return keep + __shfl_xor_sync(0xffffffffu, send, 1);
+}
+
+template <int ACC>
+__device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32, int n, int g, float fx,
+                                            float fy, float fz) {
+    if (ACC == 1) {
+        atomicAdd(F32 + g, fx);
+        atomicAdd(F32 + n + g, fy);
+        atomicAdd(F32 + 2 * n + g, fz);
+    } else {
+        atomicAdd(F64 + g, to_fixed(fx));
+        atomicAdd(F64 + n + g, to_fixed(fy));
+        atomicAdd(F64 + 2 * n + g, to_fixed(fz));
+    }
+}
+
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP>
+__global__ void __launch_bounds__(kFT, 4)
+k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
+        const int *__restrict__ cstart, Geom g, TableDev tab, const float4 *__restrict__ pcoef,
+        int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
+        float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout) {
+    extern __shared__ float4 smem[];
+    float4 *sIp = smem;
+    float4 *sJp = sIp + kChunk;
+    float4 *sCoef = sJp + kChunk;
+    int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
+    int *sJt = sIt + kChunk;
+    float *sF = reinterpret_cast<float *>(sJt + kChunk);             /* [kFW][2][3][kChunk] */
+    int *sC = reinterpret_cast<int *>(sF + kFW * 6 * kChunk);       /* [kFW][2][kChunk] */
+    __shared__ double s_red[kFW][3];
+    __shared__ unsigned long long s_cnt[kFW][2];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int row = lane >> 3, col = lane & 7;
+    const int unit = blockIdx.x;
+    const int h = unit / kHalfShellCells, f = unit - h * kHalfShellCells;
+    const int nyz = g.nc[1] * g.nc[2];
+    const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
+    int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
+    /* neighbour across the +L face: its particles sit at x + L, so d = xi - xj - L */
+    const float sx = cx >= g.nc[0] ? -g.L[0] : (cx < 0 ? g.L[0] : 0.0f);
+    const float sy = cy >= g.nc[1] ? -g.L[1] : (cy < 0 ? g.L[1] : 0.0f);
+    const float sz = cz >= g.nc[2] ? -g.L[2] : (cz < 0 ? g.L[2] : 0.0f);
+    cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
+    cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
+    cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
+    const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
+    const bool self = (f == 0);
+    const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
+    const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
+    const bool coul = ke != 0.0f;
+    const float nan = __int_as_float(0x7fc00000);
+    float *wFi = sF + warp * 6 * kChunk;
+    float *wFj = wFi + 3 * kChunk;
+    int *wCi = sC + warp * 2 * kChunk;
+    int *wCj = wCi + kChunk;
+
+    for (int t = tid; t < ntypes * ntypes; t += kFT) sCoef[t] = pcoef[t];
+
+    float acc_elj = 0.0f, acc_ec = 0.0f, acc_vir = 0.0f;
+    unsigned acc_pairs = 0, acc_below = 0;
+
+    for (int i0 = 0; i0 < ni_all; i0 += kChunk) {
+        for (int j0 = self ? i0 : 0; j0 < nj_all; j0 += kChunk) {
+            const int ni = min(kChunk, ni_all - i0), nj = min(kChunk, nj_all - j0);
+            const bool diag = self && (i0 == j0);
+            __syncthreads();
+            for (int t = tid; t < ni; t += kFT) {
+                sIp[t] = pos[hs + i0 + t];
+                sIt[t] = ptype[hs + i0 + t] * ntypes;
+            }
+            for (int t = tid; t < nj; t += kFT) {
+                sJp[t] = pos[cs + j0 + t];
+                sJt[t] = ptype[cs + j0 + t];
+            }
+            for (int t = tid; t < kFW * 6 * kChunk; t += kFT) sF[t] = 0.0f;
+            if (EXTRA)
+                for (int t = tid; t < kFW * 2 * kChunk; t += kFT) sC[t] = 0;
+            __syncthreads();
+
+            const int nti = (ni + 31) >> 5;
+            const int S = (nj + 7) >> 3;                         /* j-steps of 8 */
+            /* pieces: tile ti covers steps [first(ti), S) in runs of kStepsPerPiece */
+            int npieces = 0;
+            for (int ti = 0; ti < nti; ++ti) {
+                const int first = diag ? 4 * ti : 0;
+                npieces += (S - first + kStepsPerPiece - 1) / kStepsPerPiece;
+            }
+            for (int p = warp; p < npieces; p += kFW) {
+                int ti = 0, r = p, first = 0, cnt = 0;
+                for (;; ++ti) {
+                    first = diag ? 4 * ti : 0;
+                    cnt = (S - first + kStepsPerPiece - 1) / kStepsPerPiece;
+                    if (r < cnt) break;
+                    r -= cnt;
+                }
+                const int s0 = first + r * kStepsPerPiece;
+                const int s1 = min(S, s0 + kStepsPerPiece);
+                float xi[8], yi[8], zi[8], qi[8];
+                int tti[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int il = ti * 32 + row + 4 * k;
+                    if (il < ni) {
+                        const float4 pp = sIp[il];
+                        xi[k] = pp.x; yi[k] = pp.y; zi[k] = pp.z;
+                        qi[k] = __fmul_rn(ke, pp.w);
+                        tti[k] = sIt[il];
+                    } else {
+                        xi[k] = nan; yi[k] = nan; zi[k] = nan; qi[k] = 0.0f; tti[k] = 0;
+                    }
+                }
+                float fi[24];
+#pragma unroll
+                for (int t = 0; t < 24; ++t) fi[t] = 0.0f;
+                int ci[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int s = s0; s < s1; ++s) {
+                    const int jl = s * 8 + col;
+                    float xj = nan, yj = nan, zj = nan, qj = 0.0f;
+                    int ttj = 0;
+                    if (jl < nj) {
+                        const float4 pp = sJp[jl];
+                        xj = pp.x; yj = pp.y; zj = pp.z; qj = pp.w;
+                        ttj = sJt[jl];
+                    }
+                    float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+                    int cj = 0;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
+                        const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
+                        const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                   __fmul_rn(dz, dz));
+                        bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
+                        if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
+                        if (ok) {
+                            float v14, v8, v3, v12, v6, v1;
+                            pair_functions_fast<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1);
+                            const float4 pc = sCoef[tti[k] + ttj];
+                            const float qq = __fmul_rn(qi[k], qj);
+                            const float fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
+                            const float fx = __fmul_rn(fs, dx), fy = __fmul_rn(fs, dy), fz = __fmul_rn(fs, dz);
+                            fi[3 * k] += fx; fi[3 * k + 1] += fy; fi[3 * k + 2] += fz;
+                            fjx -= fx; fjy -= fy; fjz -= fz;
+                            ++acc_pairs;
+                            if (EXTRA) {
+                                ++ci[k];
+                                ++cj;
+                                acc_below += (ORDER > 0 && r2 < tab.r2min) ? 1u : 0u;
+                                acc_elj += combine_elj<SEP>(pc, v12, v6);
+                                if (coul) acc_ec += __fmul_rn(qq, v1);
+                                acc_vir += __fmul_rn(fs, r2);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int o = 8; o < 32; o <<= 1) {
+                        fjx += __shfl_xor_sync(0xffffffffu, fjx, o);
+                        fjy += __shfl_xor_sync(0xffffffffu, fjy, o);
+                        fjz += __shfl_xor_sync(0xffffffffu, fjz, o);
+                        if (EXTRA) cj += __shfl_xor_sync(0xffffffffu, cj, o);
+                    }
+                    if (row == 0 && jl < nj) {
+                        wFj[jl] += fjx;
+                        wFj[kChunk + jl] += fjy;
+                        wFj[2 * kChunk + jl] += fjz;
+                        if (EXTRA) wCj[jl] += cj;
+                    }
+                }
+                reduce_scatter24(fi, col);
+                int cnt_i = 0;
+                if (EXTRA) cnt_i = reduce_scatter8i(ci, col);
+                const int il = ti * 32 + row + 4 * col;
+                if (il < ni) {
+                    wFi[il] += fi[0];
+                    wFi[kChunk + il] += fi[1];
+                    wFi[2 * kChunk + il] += fi[2];
+                    if (EXTRA) wCi[il] += cnt_i;
+                }
+            }
+            __syncthreads();
+            /* sum the warp accumulators in warp order; one atomic per particle and component */
+            for (int t = tid; t < ni; t += kFT) {
+                float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+                int cc = 0;
+#pragma unroll
+                for (int w = 0; w < kFW; ++w) {
+                    const float *a = sF + w * 6 * kChunk;
+                    v0 += a[t]; v1 += a[kChunk + t]; v2 += a[2 * kChunk + t];
+                    if (diag) { v0 += a[3 * kChunk + t]; v1 += a[4 * kChunk + t]; v2 += a[5 * kChunk + t]; }
+                    if (EXTRA) cc += sC[w * 2 * kChunk + t] + (diag ? sC[w * 2 * kChunk + kChunk + t] : 0);
+                }
+                flush_force<ACC>(F64, F32, n, hs + i0 + t, v0, v1, v2);
+                if (EXTRA && cc) atomicAdd(counts + hs + i0 + t, cc);
+            }
+            if (!diag) {
+                for (int t = tid; t < nj; t += kFT) {
+                    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+                    int cc = 0;
+#pragma unroll
+                    for (int w = 0; w < kFW; ++w) {
+                        const float *a = sF + w * 6 * kChunk + 3 * kChunk;
+                        v0 += a[t]; v1 += a[kChunk + t]; v2 += a[2 * kChunk + t];
+                        if (EXTRA) cc += sC[w * 2 * kChunk + kChunk + t];
+                    }
+                    flush_force<ACC>(F64, F32, n, cs + j0 + t, v0, v1, v2);
+                    if (EXTRA && cc) atomicAdd(counts + cs + j0 + t, cc);
+                }
+            }
+        }
+    }
+
+    double e1 = acc_elj, e2 = acc_ec, e3 = acc_vir;
+    unsigned long long c1 = acc_pairs, c2 = acc_below;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        if (EXTRA) {
+            e1 += __shfl_xor_sync(0xffffffffu, e1, o);
+            e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+            e3 += __shfl_xor_sync(0xffffffffu, e3, o);
+            c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        }
+    }
+    if (lane == 0) {
+        s_red[warp][0] = e1; s_red[warp][1] = e2; s_red[warp][2] = e3;
+        s_cnt[warp][0] = c1; s_cnt[warp][1] = c2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        UnitOut u;
+        u.e_lj = u.e_coul = u.virial = 0.0;
+        u.pairs = u.below = 0ull;
+        for (int w = 0; w < kFW; ++w) {
+            u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
+            u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
+        }
+        uout[unit] = u;
+    }
+}
+
+}  // namespace mdrl

@@ -42,7 +42,7 @@ __constant__ int c_halfshell[kHalfShellCells][3] = {
     {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},  {1, 1, -1}, {1, 1, 0},   {1, 1, 1}};
 
 /* Error bits raised by kernels and read by the host after a call. */
-enum : unsigned { kErrPosition = 1u };
+enum : unsigned { kErrPosition = 1u, kErrType = 2u };
 
 struct MassTab {
     float cm[MDRL_MAX_TYPES];   /* velocity increment per unit force for the kick */
@@ -174,7 +174,7 @@ __device__ __forceinline__ bool in_box(const Geom &g, float x, float y, float z)
 }
 
 /* Cell of each user-order particle, with its arrival slot in the cell. */
-__global__ void k_bin_user(int n, const float *__restrict__ x, const float *__restrict__ y,
+static __global__ void k_bin_user(int n, const float *__restrict__ x, const float *__restrict__ y,
                            const float *__restrict__ z, Geom g, int *__restrict__ cell_of,
                            int *__restrict__ slot, int *__restrict__ count,
                            unsigned *__restrict__ err) {
@@ -188,7 +188,7 @@ __global__ void k_bin_user(int n, const float *__restrict__ x, const float *__re
 }
 
 /* Exclusive scan of the cell counts (one CTA), plus the largest occupancy. */
-__global__ void __launch_bounds__(1024) k_scan(int ncells, const int *__restrict__ count,
+static __global__ void __launch_bounds__(1024) k_scan(int ncells, const int *__restrict__ count,
                                                int *__restrict__ start, DevTotals *tot) {
     __shared__ int s_sum[1024];
     __shared__ int s_max[1024];
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(1024) k_scan(int ncells, const int *__restrict
     if (t == 1023) { start[ncells] = s_sum[1023]; tot->max_occ = s_max[1023]; }
 }
 
-__global__ void k_scatter(int n, const int *__restrict__ cell_of, const int *__restrict__ slot,
+static __global__ void k_scatter(int n, const int *__restrict__ cell_of, const int *__restrict__ slot,
                           const int *__restrict__ start, int *__restrict__ tmp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -221,7 +221,7 @@ __global__ void k_scatter(int n, const int *__restrict__ cell_of, const int *__r
 }
 
 /* Order each cell's ids ascending: the rank of an id is the number of smaller ids in its cell. */
-__global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start,
+static __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start,
                                                    const int *__restrict__ tmp,
                                                    int *__restrict__ sorted) {
     __shared__ int s_ids[1024];
@@ -243,292 +243,28 @@ __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start
 }
 
 /* Gather user-order inputs into cell order and clear the force accumulators. */
-__global__ void k_gather_user(int n, const int *__restrict__ sorted, const float *__restrict__ x,
+static __global__ void k_gather_user(int n, const int *__restrict__ sorted, const float *__restrict__ x,
                               const float *__restrict__ y, const float *__restrict__ z,
                               const float *__restrict__ q, const int *__restrict__ type,
                               float4 *__restrict__ pos, int *__restrict__ ptype,
                               int *__restrict__ pid, unsigned long long *__restrict__ F64,
-                              float *__restrict__ F32, int *__restrict__ counts) {
+                              float *__restrict__ F32, int *__restrict__ counts, int ntypes,
+                              unsigned *__restrict__ err) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = sorted[k];
     pos[k] = make_float4(x[id], y[id], z[id], q ? q[id] : 0.0f);
-    ptype[k] = type ? type[id] : 0;
+    int t = type ? type[id] : 0;
+    if (t < 0 || t >= ntypes) { atomicOr(err, kErrType); t = 0; }
+    ptype[k] = t;
     pid[k] = id;
     if (F64) { F64[k] = 0ull; F64[n + k] = 0ull; F64[2 * n + k] = 0ull; }
     if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
     if (counts) counts[k] = 0;
 }
 
-/* ------------------------------------------------------------------------------------------ */
-/* Half-shell force.  One CTA per unit (home cell h, half-shell neighbour f): the CTA stages
- * h's and the neighbour's particles in shared memory (256 at a time) and its 8 warps split the
- * (i, j) square into 32 x 32 pieces.  In a piece, lane (row, col) holds i = row + 8k (k < 4)
- * in registers and takes j = 4*step + col; the j force of a step is reduced over the 8 rows
- * with shuffles and added to the warp's private shared-memory accumulator, the i force is
- * summed in registers over the piece and reduced over the 4 columns.  At the end of the unit
- * the 8 warp accumulators are summed in warp order, converted to int64 fixed point and added
- * to global memory with one atomic per particle and component.  Every FP32 sum has a fixed
- * order, and the int64 sums are exact, so forces are bit-reproducible run to run.
- * For the home cell itself (f = 0) only pairs i < j in cell order are taken.                 */
-
-template <int ORDER, bool SEP, bool EXTRA, int ACC>
-__global__ void __launch_bounds__(kThreads, 2)
-k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
-        const int *__restrict__ cstart, Geom g, TableDev tab, const float4 *__restrict__ pcoef,
-        int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
-        float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout) {
-    extern __shared__ float4 smem[];
-    float4 *sIp = smem;
-    float4 *sJp = sIp + kChunk;
-    float4 *sCoef = sJp + kChunk;                                      /* [ntypes^2] */
-    int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
-    int *sJt = sIt + kChunk;
-    float *sFi = reinterpret_cast<float *>(sJt + kChunk);              /* [kWarps][3][kChunk] */
-    float *sFj = sFi + kWarps * 3 * kChunk;
-    int *sCi = reinterpret_cast<int *>(sFj + kWarps * 3 * kChunk);     /* EXTRA: [kWarps][kChunk] */
-    int *sCj = sCi + kWarps * kChunk;
-    __shared__ double s_red[kWarps][3];
-    __shared__ unsigned long long s_cnt[kWarps][2];
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int row = lane >> 2, col = lane & 3;
-    const int unit = blockIdx.x;
-    const int h = unit / kHalfShellCells, f = unit - h * kHalfShellCells;
-    const int nyz = g.nc[1] * g.nc[2];
-    const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
-    int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
-    cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
-    cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
-    cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
-    const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
-    const bool self = (f == 0);
-    const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
-    const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
-    const bool coul = ke != 0.0f;
-    const float nan = __int_as_float(0x7fc00000);
-
-    for (int t = tid; t < ntypes * ntypes; t += kThreads) sCoef[t] = pcoef[t];
-
-    float acc_elj = 0.0f, acc_ec = 0.0f, acc_vir = 0.0f;
-    unsigned acc_pairs = 0, acc_below = 0;
-
-    for (int i0 = 0; i0 < ni_all; i0 += kChunk) {
-        for (int j0 = self ? i0 : 0; j0 < nj_all; j0 += kChunk) {
-            const int ni = min(kChunk, ni_all - i0), nj = min(kChunk, nj_all - j0);
-            const bool diag = self && (i0 == j0);
-            __syncthreads();
-            for (int t = tid; t < ni; t += kThreads) {
-                sIp[t] = pos[hs + i0 + t];
-                sIt[t] = ptype[hs + i0 + t] * ntypes;
-            }
-            for (int t = tid; t < nj; t += kThreads) {
-                sJp[t] = pos[cs + j0 + t];
-                sJt[t] = ptype[cs + j0 + t];
-            }
-            for (int t = tid; t < kWarps * 3 * kChunk; t += kThreads) { sFi[t] = 0.0f; sFj[t] = 0.0f; }
-            if (EXTRA)
-                for (int t = tid; t < kWarps * kChunk; t += kThreads) { sCi[t] = 0; sCj[t] = 0; }
-            __syncthreads();
-
-            const int nti = (ni + 31) >> 5, ntj = (nj + 31) >> 5;
-            const int npieces = diag ? nti * (nti + 1) / 2 : nti * ntj;
-            float *wFi = sFi + warp * 3 * kChunk;
-            float *wFj = sFj + warp * 3 * kChunk;
-            int *wCi = sCi + warp * kChunk;
-            int *wCj = sCj + warp * kChunk;
-            for (int p = warp; p < npieces; p += kWarps) {
-                int ti, tj;
-                if (diag) {
-                    int r = p;
-                    ti = 0;
-                    while (r >= nti - ti) { r -= nti - ti; ++ti; }
-                    tj = ti + r;
-                } else {
-                    ti = p / ntj;
-                    tj = p - ti * ntj;
-                }
-                float xi[4], yi[4], zi[4], qi[4];
-                int tti[4], il[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    il[k] = ti * 32 + row + 8 * k;
-                    if (il[k] < ni) {
-                        const float4 pp = sIp[il[k]];
-                        xi[k] = pp.x; yi[k] = pp.y; zi[k] = pp.z;
-                        qi[k] = __fmul_rn(ke, pp.w);
-                        tti[k] = sIt[il[k]];
-                    } else {
-                        xi[k] = nan; yi[k] = nan; zi[k] = nan; qi[k] = 0.0f; tti[k] = 0;
-                    }
-                }
-                float fix[4] = {0.f, 0.f, 0.f, 0.f}, fiy[4] = {0.f, 0.f, 0.f, 0.f},
-                      fiz[4] = {0.f, 0.f, 0.f, 0.f};
-                int ci[4] = {0, 0, 0, 0};
-#pragma unroll 2
-                for (int s = 0; s < 8; ++s) {
-                    const int jl = tj * 32 + s * 4 + col;
-                    float xj = nan, yj = nan, zj = nan, qj = 0.0f;
-                    int ttj = 0;
-                    if (jl < nj) {
-                        const float4 pp = sJp[jl];
-                        xj = pp.x; yj = pp.y; zj = pp.z; qj = pp.w;
-                        ttj = sJt[jl];
-                    }
-                    float fjx = 0.f, fjy = 0.f, fjz = 0.f;
-                    int cj = 0;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const float dx = wrap_d(__fsub_rn(xi[k], xj), g.L[0], g.h[0]);
-                        const float dy = wrap_d(__fsub_rn(yi[k], yj), g.L[1], g.h[1]);
-                        const float dz = wrap_d(__fsub_rn(zi[k], zj), g.L[2], g.h[2]);
-                        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
-                                                   __fmul_rn(dz, dz));
-                        bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
-                        if (diag) ok = ok && (il[k] < jl);
-                        if (ok) {
-                            float v14, v8, v3, v12, v6, v1;
-                            int below;
-                            pair_functions<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1,
-                                                              below);
-                            const float4 pc = sCoef[tti[k] + ttj];
-                            const float qq = __fmul_rn(qi[k], qj);
-                            const float fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
-                            const float fx = __fmul_rn(fs, dx), fy = __fmul_rn(fs, dy),
-                                        fz = __fmul_rn(fs, dz);
-                            fix[k] += fx; fiy[k] += fy; fiz[k] += fz;
-                            fjx -= fx; fjy -= fy; fjz -= fz;
-                            ++acc_pairs;
-                            if (EXTRA) {
-                                ++ci[k];
-                                ++cj;
-                                acc_below += below;
-                                acc_elj += combine_elj<SEP>(pc, v12, v6);
-                                if (coul) acc_ec += __fmul_rn(qq, v1);
-                                acc_vir += __fmul_rn(fs, r2);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int o = 4; o < 32; o <<= 1) {
-                        fjx += __shfl_xor_sync(0xffffffffu, fjx, o);
-                        fjy += __shfl_xor_sync(0xffffffffu, fjy, o);
-                        fjz += __shfl_xor_sync(0xffffffffu, fjz, o);
-                        if (EXTRA) cj += __shfl_xor_sync(0xffffffffu, cj, o);
-                    }
-                    if (row == 0 && jl < nj) {
-                        wFj[jl] += fjx;
-                        wFj[kChunk + jl] += fjy;
-                        wFj[2 * kChunk + jl] += fjz;
-                        if (EXTRA) wCj[jl] += cj;
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-#pragma unroll
-                    for (int o = 1; o < 4; o <<= 1) {
-                        fix[k] += __shfl_xor_sync(0xffffffffu, fix[k], o);
-                        fiy[k] += __shfl_xor_sync(0xffffffffu, fiy[k], o);
-                        fiz[k] += __shfl_xor_sync(0xffffffffu, fiz[k], o);
-                        if (EXTRA) ci[k] += __shfl_xor_sync(0xffffffffu, ci[k], o);
-                    }
-                    if (col == 0 && il[k] < ni) {
-                        wFi[il[k]] += fix[k];
-                        wFi[kChunk + il[k]] += fiy[k];
-                        wFi[2 * kChunk + il[k]] += fiz[k];
-                        if (EXTRA) wCi[il[k]] += ci[k];
-                    }
-                }
-            }
-            __syncthreads();
-            /* Flush: sum the warp accumulators in warp order, then one atomic per component. */
-            for (int t = tid; t < ni; t += kThreads) {
-                float v[3];
-                int cc = 0;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    float sacc = 0.0f;
-                    for (int w = 0; w < kWarps; ++w) {
-                        sacc += sFi[(w * 3 + d) * kChunk + t];
-                        if (diag) sacc += sFj[(w * 3 + d) * kChunk + t];
-                    }
-                    v[d] = sacc;
-                }
-                if (EXTRA)
-                    for (int w = 0; w < kWarps; ++w) cc += sCi[w * kChunk + t] + (diag ? sCj[w * kChunk + t] : 0);
-                const int gi = hs + i0 + t;
-                if (ACC == 1) {
-                    atomicAdd(F32 + gi, v[0]); atomicAdd(F32 + n + gi, v[1]); atomicAdd(F32 + 2 * n + gi, v[2]);
-                } else {
-                    atomicAdd(F64 + gi, to_fixed(v[0]));
-                    atomicAdd(F64 + n + gi, to_fixed(v[1]));
-                    atomicAdd(F64 + 2 * n + gi, to_fixed(v[2]));
-                }
-                if (EXTRA && cc) atomicAdd(counts + gi, cc);
-            }
-            if (!diag) {
-                for (int t = tid; t < nj; t += kThreads) {
-                    float v[3];
-                    int cc = 0;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        float sacc = 0.0f;
-                        for (int w = 0; w < kWarps; ++w) sacc += sFj[(w * 3 + d) * kChunk + t];
-                        v[d] = sacc;
-                    }
-                    if (EXTRA)
-                        for (int w = 0; w < kWarps; ++w) cc += sCj[w * kChunk + t];
-                    const int gj = cs + j0 + t;
-                    if (ACC == 1) {
-                        atomicAdd(F32 + gj, v[0]); atomicAdd(F32 + n + gj, v[1]); atomicAdd(F32 + 2 * n + gj, v[2]);
-                    } else {
-                        atomicAdd(F64 + gj, to_fixed(v[0]));
-                        atomicAdd(F64 + n + gj, to_fixed(v[1]));
-                        atomicAdd(F64 + 2 * n + gj, to_fixed(v[2]));
-                    }
-                    if (EXTRA && cc) atomicAdd(counts + gj, cc);
-                }
-            }
-        }
-    }
-
-    /* Unit totals: lane -> warp (shuffles) -> CTA (warp order) -> one slot per unit. */
-    double e1 = acc_elj, e2 = acc_ec, e3 = acc_vir;
-    unsigned long long c1 = acc_pairs, c2 = acc_below;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
-        if (EXTRA) {
-            e1 += __shfl_xor_sync(0xffffffffu, e1, o);
-            e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-            e3 += __shfl_xor_sync(0xffffffffu, e3, o);
-            c2 += __shfl_xor_sync(0xffffffffu, c2, o);
-        }
-    }
-    if (lane == 0) {
-        s_red[warp][0] = e1; s_red[warp][1] = e2; s_red[warp][2] = e3;
-        s_cnt[warp][0] = c1; s_cnt[warp][1] = c2;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        UnitOut u;
-        u.e_lj = u.e_coul = u.virial = 0.0;
-        u.pairs = u.below = 0ull;
-        for (int w = 0; w < kWarps; ++w) {
-            u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
-            u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
-        }
-        uout[unit] = u;
-    }
-}
-
-inline size_t force_smem_bytes(int ntypes) {
-    return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
-           sizeof(float) * 2 * kWarps * 3 * kChunk + sizeof(int) * 2 * kWarps * kChunk;
-}
-
 /* Totals over units and kinetic-energy partials, in a fixed order (one CTA). */
-__global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__restrict__ uout,
+static __global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__restrict__ uout,
                                                 int nke, const double *__restrict__ kepart,
                                                 DevTotals *tot) {
     __shared__ double s_d[256][4];
@@ -561,7 +297,7 @@ __global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__res
 }
 
 /* Sorted forces back to user order as float (and counts). */
-__global__ void k_unsort(int n, const int *__restrict__ pid, const unsigned long long *__restrict__ F64,
+static __global__ void k_unsort(int n, const int *__restrict__ pid, const unsigned long long *__restrict__ F64,
                          const float *__restrict__ F32, const int *__restrict__ cnt_s,
                          float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ fz,
                          int *__restrict__ cnt_u) {
@@ -595,7 +331,7 @@ __device__ __forceinline__ float force_of(const unsigned long long *F64, const f
 }
 
 /* v += F * cm[type] (half or full kick), x += v * dt, wrap, and bin the new position. */
-__global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
+static __global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                  const int *__restrict__ ptype,
                                  const unsigned long long *__restrict__ F64,
                                  const float *__restrict__ F32, MassTab mt, float dt, Geom g,
@@ -620,7 +356,7 @@ __global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 *__rest
 }
 
 /* Reorder the state into the new cell order and clear the force accumulators. */
-__global__ void k_gather_state(int n, const int *__restrict__ sorted,
+static __global__ void k_gather_state(int n, const int *__restrict__ sorted,
                                const float4 *__restrict__ pos0, const float4 *__restrict__ vel0,
                                const int *__restrict__ type0, const int *__restrict__ id0,
                                float4 *__restrict__ pos1, float4 *__restrict__ vel1,
@@ -638,7 +374,7 @@ __global__ void k_gather_state(int n, const int *__restrict__ sorted,
 }
 
 /* Second half kick (velocity Verlet) and per-block kinetic energy partials. */
-__global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, const int *__restrict__ ptype,
+static __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, const int *__restrict__ ptype,
                                               const unsigned long long *__restrict__ F64,
                                               const float *__restrict__ F32, MassTab mt, int do_kick,
                                               double *__restrict__ kepart) {
@@ -669,7 +405,7 @@ __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, c
 }
 
 /* Sorted state back to user order. */
-__global__ void k_unsort_state(int n, const int *__restrict__ pid, const float4 *__restrict__ pos,
+static __global__ void k_unsort_state(int n, const int *__restrict__ pid, const float4 *__restrict__ pos,
                                const float4 *__restrict__ vel, float *__restrict__ x,
                                float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
                                float *__restrict__ vy, float *__restrict__ vz) {
@@ -682,7 +418,7 @@ __global__ void k_unsort_state(int n, const int *__restrict__ pid, const float4 
 }
 
 /* Gather user-order velocities into cell order (set_state). */
-__global__ void k_gather_vel(int n, const int *__restrict__ pid, const float *__restrict__ vx,
+static __global__ void k_gather_vel(int n, const int *__restrict__ pid, const float *__restrict__ vx,
                              const float *__restrict__ vy, const float *__restrict__ vz,
                              float4 *__restrict__ vel) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -695,7 +431,7 @@ __global__ void k_gather_vel(int n, const int *__restrict__ pid, const float *__
 /* Per-pair evaluation: the drop-in for the OpenCL library function RL_LJ_Evaluation.          */
 
 template <int ORDER, bool SEP>
-__global__ void k_pair_eval(int n, const float4 *__restrict__ ref, const float4 *__restrict__ nbr,
+static __global__ void k_pair_eval(int n, const float4 *__restrict__ ref, const float4 *__restrict__ nbr,
                             const int *__restrict__ tref, const int *__restrict__ tnbr, Geom g,
                             TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke,
                             float4 *__restrict__ out, float2 *__restrict__ aux) {

@@ -15,7 +15,8 @@ from helpers import force_err, kat1, kat2_positions, oracle_from_ctx
 
 pytestmark = pytest.mark.gpu
 
-SUM_TOL = 2e-6     # |F_gpu - F_oracle| <= SUM_TOL * sum_j |f_ij|, per particle and component
+SUM_TOL = 2e-6     # |F_gpu - F_oracle| <= SUM_TOL * sum_j |f_ij| + FIX_ABS, per particle and component
+FIX_ABS = 64 * 2.0 ** -24   # int64 fixed point: each of a particle's per-unit flushes rounds to 2^-24
 
 
 def test_pair_eval_kat1_bit_exact():
@@ -94,8 +95,8 @@ def _check_force(sysm, params, tol=SUM_TOL):
     assert np.array_equal(cnt, cnto), "partner counts differ"
     assert st["pairs"] == sto["pairs"]
     assert st["below_table"] == sto["below_table"]
-    err = np.abs(F - Fo) / np.maximum(Fabs, 1e-30)
-    assert err.max() <= tol, f"max |dF|/sum|f| = {err.max():.3e}"
+    err = np.abs(F - Fo) / (tol * Fabs + FIX_ABS)
+    assert err.max() <= 1.0, f"max |dF| / (tol*sum|f| + fixed-point quantum) = {err.max():.3e}"
     if params.accum == m.ACC_FIXED64:
         assert np.array_equal(F.view(np.uint32), F2.view(np.uint32)), "not bit-reproducible"
     for key in ("e_lj", "e_coul", "virial"):
@@ -115,19 +116,21 @@ def test_force_small_ljc(order, bins, arith):
 
 def test_force_lj1728_and_fp64_error():
     """The 1,728-atom LJ argon cube (3x3x3 cells): parity with the oracle, and the stated force
-    error of 1st-order 512-bin tables against the FP64 direct oracle."""
+    error of 1st-order 1024-bin tables against the FP64 direct oracle (median per-particle
+    relative error <= 1e-5; max error over the rms force <= 2e-5)."""
     sysm = systems.lj1728()
-    p = sysm.params(table_bins=512, flags=m.FLAG_ENERGY)
+    p = sysm.params(table_bins=1024, flags=m.FLAG_ENERGY)
     F, Fo, o = _check_force(sysm, p)
     F64, _ = o.force_direct64()
     emax, emed = force_err(F, F64)
     assert emed <= 1e-5, emed
-    assert emax <= 1e-3, emax
+    assert emax <= 2e-5, emax
 
 
-def test_force_ljc_fp64_error_512_bins():
+def test_force_ljc_fp64_error_1024_bins():
+    """LJ+Coulomb, 4 types: median per-particle relative error against FP64 direct <= 1e-5."""
     sysm = systems.small_ljc(6000, 49.6, 12.0, seed=5)
-    p = sysm.params(table_bins=512)
+    p = sysm.params(table_bins=1024)
     with m.Context(p) as ctx:
         F, st, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
         o = oracle_from_ctx(ctx, sysm)
@@ -146,8 +149,9 @@ def test_force_large_cell_chunks():
     """A cell holding more particles than one shared-memory chunk (256) is processed in chunks."""
     rng = np.random.default_rng(8)
     L = 30.0
-    pos = rng.uniform(0, L, (1500, 3)).astype(np.float32)
-    pos[:700] = rng.uniform(0, 10.0, (700, 3)).astype(np.float32)   # > 256 in cell (0,0,0)
+    dense = systems.uniform_min_sep(700, (9.9, 9.9, 9.9), 0.45, rng)          # 700 in cell (0,0,0)
+    rest = systems.uniform_min_sep(800, (19.0, 30.0, 30.0), 0.45, rng) + np.array([10.5, 0.0, 0.0])
+    pos = systems.wrap_into_box(np.concatenate([dense, rest]), (L, L, L))
     sysm = systems.System("dense", (L, L, L), 10.0, (3, 3, 3), pos, np.zeros_like(pos), None,
                           np.zeros(1500, np.int32), [0.5], [0.01], [39.95], 0.0)
     p = sysm.params(table_min_log2=-8)
@@ -156,7 +160,7 @@ def test_force_large_cell_chunks():
         o = oracle_from_ctx(ctx, sysm)
     Fo, Fabs, cnto, sto = o.force_cells()
     assert np.array_equal(cnt, cnto)
-    assert (np.abs(F - Fo) / np.maximum(Fabs, 1e-30)).max() <= SUM_TOL
+    assert (np.abs(F - Fo) / (SUM_TOL * Fabs + FIX_ABS)).max() <= 1.0
 
 
 def test_edge_cases():
@@ -176,6 +180,9 @@ def test_edge_cases():
         assert e.value.status == 1
         with pytest.raises(m.MdrlError):
             ctx.force([np.nan], [1.0], [1.0])
+        with pytest.raises(m.MdrlError) as e:
+            ctx.force([1.0], [1.0], [1.0], type=[5])
+        assert e.value.status == 1 and "types" in str(e.value)
     with pytest.raises(m.MdrlError) as e:
         with m.Context(m.default_params(box=(16.0, 25.5, 25.5))) as ctx:   # 1 cell of 16 A on x
             ctx.force([1.0], [1.0], [1.0])
