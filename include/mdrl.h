@@ -193,6 +193,22 @@ mdrl_status mdrl_get_state(mdrl_ctx *ctx, float *x, float *y, float *z, float *v
  * context's stream; *ms receives the kernel's device time.  The state is not modified. */
 mdrl_status mdrl_time_force(mdrl_ctx *ctx, float *ms);
 
+/* One force evaluation that allocates no memory; it has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a device owned by another allocator or memory pool,
+ * a plugin host that forbids allocations, a loop that cannot pay for a first-use allocation):
+ * no context is needed, and all scratch (cell lists, sorted particles, int64 accumulators,
+ * reduction slots, tables) lives in one 16 MiB static device array that every GPU loading the
+ * library holds until the process exits.  x, y, z, q, type and fx, fy, fz are DEVICE pointers
+ * (q and type may be NULL); stream is a cudaStream_t (NULL = the legacy default stream); the
+ * call synchronises that stream.  *pairs_out (optional) receives the number of pairs.
+ * Limits: n <= 131072, <= 8192 cells, nseg * bins <= 16384, MDRL_ACC_FIXED64 only; beyond them
+ * the call returns MDRL_ERR_RANGE.  The first call on a device looks up the array's device
+ * address (make it before any stream capture).  All calls share the array and it keeps the last
+ * call's contents: calls whose GPU work overlaps race and must be serialised by the caller. */
+mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const float *x, const float *y,
+                                   const float *z, const float *q, const int *type, float *fx,
+                                   float *fy, float *fz, int64_t *pairs_out, void *stream);
+
 /* Drop-in for the reference C model's entry point.  Reads the argon PDB named by the
  * environment variable MDRL_INPUT (N from MDRL_N, default 500; iterations from MDRL_ITERS,
  * default 100), runs the reference's all-pairs direct FP32 force and symplectic-Euler update on

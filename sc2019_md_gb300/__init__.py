@@ -101,13 +101,15 @@ def lib() -> C.CDLL:
     L.mdrl_step.argtypes = [vp, st, C.POINTER(Stats)]
     L.mdrl_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
     L.mdrl_time_force.argtypes = [vp, _F]
+    L.mdrl_force_eval_static.argtypes = [C.POINTER(Params), st, vp, vp, vp, vp, vp, vp, vp, vp,
+                                         C.POINTER(C.c_int64), vp]
     L.MD_Evaluation_Model.argtypes = []
     L.MD_Evaluation_Model.restype = C.c_int
     L.mdrl_cmodel_run.argtypes = [st, st, C.c_float, C.c_float, _F, _F, _F, _I]
     for name in ("mdrl_fit_tables", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
                  "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
                  "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
-                 "mdrl_get_state", "mdrl_cmodel_run", "mdrl_time_force"):
+                 "mdrl_get_state", "mdrl_cmodel_run", "mdrl_time_force", "mdrl_force_eval_static"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -286,6 +288,16 @@ class Context:
         a = [np.zeros(n, np.float32) for _ in range(9)]
         _check(lib().mdrl_get_state(self._h, *[_fp(v) for v in a]))
         return (np.stack(a[0:3], 1), np.stack(a[3:6], 1), np.stack(a[6:9], 1))
+
+
+def force_eval_static(params: Params, n: int, x, y, z, q, type, fx, fy, fz, stream=None) -> int:
+    """mdrl_force_eval_static: a force evaluation that allocates no device memory.  Every array
+    argument is a device address (an int, e.g. a torch tensor's data_ptr(), or None for q/type);
+    returns the number of pairs."""
+    pairs = C.c_int64()
+    _check(lib().mdrl_force_eval_static(C.byref(params), n, x, y, z, q, type, fx, fy, fz,
+                                        C.byref(pairs), stream))
+    return pairs.value
 
 
 def cmodel_run(pos: np.ndarray, vel: np.ndarray, iters: int, box: float = 24.0,
