@@ -4,7 +4,7 @@
 A step is one velocity-Verlet MD step of the whole system on the GPU: kick + drift + rebin
 (count, scan, scatter, in-cell sort, gather), the half-shell force kernel, kick.  Default
 workload: the 92,224-atom LJ+Coulomb system (108.86 x 108.86 x 77.76 A, rc 12 A, 9x9x6 cells,
-4 types, +-0.42 e) with first-order 1024-bin tables and int64 fixed-point accumulation ("tuned"),
+4 types, +-0.42 e) with first-order 512-bin tables and int64 fixed-point accumulation ("tuned"),
 next to the FP32-atomic accumulation ("plain") at the same tables.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference] [--workload ...]
@@ -402,7 +402,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="ljc92k", choices=["ljc92k", "lj1728", "ljc1m"])
-    ap.add_argument("--bins", type=int, default=1024)
+    ap.add_argument("--bins", type=int, default=512)
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -201,7 +201,7 @@ mdrl_status mdrl_time_force(mdrl_ctx *ctx, float *ms);
  * library holds until the process exits.  x, y, z, q, type and fx, fy, fz are DEVICE pointers
  * (q and type may be NULL); stream is a cudaStream_t (NULL = the legacy default stream); the
  * call synchronises that stream.  *pairs_out (optional) receives the number of pairs.
- * Limits: n <= 131072, <= 8192 cells, nseg * bins <= 16384, MDRL_ACC_FIXED64 only; beyond them
+ * Limits: n <= 131072, <= 4096 cells, nseg * bins <= 16384, MDRL_ACC_FIXED64 only; beyond them
  * the call returns MDRL_ERR_RANGE.  The first call on a device looks up the array's device
  * address (make it before any stream capture).  All calls share the array and it keeps the last
  * call's contents: calls whose GPU work overlaps race and must be serialised by the caller. */

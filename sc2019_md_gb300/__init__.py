@@ -33,7 +33,10 @@ _HERE = Path(__file__).resolve().parent
 
 
 def library_path() -> Path:
-    return _HERE / "_build" / "libmdrl.so"
+    """The in-tree libmdrl.so, or the file named by MDRL_LIBRARY (a build variant)."""
+    import os
+    env = os.environ.get("MDRL_LIBRARY")
+    return Path(env) if env else _HERE / "_build" / "libmdrl.so"
 
 
 class MdrlError(RuntimeError):

@@ -44,40 +44,45 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
-def _compile(src: Path, ptxas_verbose: bool) -> tuple[Path, str]:
-    obj = OUT / (src.name + ".o")
+def _compile(src: Path, ptxas_verbose: bool, out: Path = OUT, defines: tuple = ()) -> tuple[Path, str]:
+    obj = out / (src.name + ".o")
+    dflags = [f"-D{d}" for d in defines]
     if src.suffix == ".cu":
-        cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *dflags, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd = ["g++", *CXX_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+        cmd = ["g++", *CXX_FLAGS, *dflags, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     return obj, res.stdout + res.stderr
 
 
-def build(force: bool = False, ptxas_verbose: bool = False) -> Path:
-    """Compile every CUDA/C++ translation unit and link libmdrl.so; returns its path."""
-    if not force and not ptxas_verbose and up_to_date():
+def build(force: bool = False, ptxas_verbose: bool = False, out_dir: Path | None = None,
+          defines: tuple = ()) -> Path:
+    """Compile every CUDA/C++ translation unit and link libmdrl.so; returns its path.  `out_dir`
+    and `defines` (-D flags) build a variant elsewhere (tuning sweeps)."""
+    out = OUT if out_dir is None else Path(out_dir)
+    lib = out / "libmdrl.so"
+    if out_dir is None and not defines and not force and not ptxas_verbose and up_to_date():
         return LIB
-    OUT.mkdir(parents=True, exist_ok=True)
+    out.mkdir(parents=True, exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        results = list(ex.map(lambda s: _compile(s, ptxas_verbose), srcs))
+        results = list(ex.map(lambda s: _compile(s, ptxas_verbose, out, defines), srcs))
     objs = [str(o) for o, _ in results]
-    tmp = OUT / "libmdrl.so.tmp"
+    tmp = out / "libmdrl.so.tmp"
     cmd = [nvcc_path(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", str(tmp), *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if ptxas_verbose:
         for _, log in results:
             if log.strip():
                 print(log)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -7,8 +7,10 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <map>
 #include <mutex>
 #include <set>
+#include <tuple>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -67,6 +69,7 @@ struct mdrl_ctx {
     float ke = 0.0f;
     float2 *d_f2 = nullptr, *d_e2 = nullptr;
     float4 *d_f4 = nullptr, *d_e4 = nullptr;
+    float4 *d_fr = nullptr;      /* order 1: force functions packed per index (32 B) */
     float4 *d_pcoef = nullptr;
     MassTab mt_half, mt_full;
 
@@ -82,6 +85,7 @@ struct mdrl_ctx {
     int cur = 0;
     int *d_cell_of = nullptr, *d_slot = nullptr, *d_tmp = nullptr, *d_sorted = nullptr;
     int *d_count = nullptr, *d_start = nullptr;
+    unsigned *d_key = nullptr;   /* in-cell sort key (Morton code inside the cell) */
     unsigned long long *d_F64 = nullptr;
     float *d_F32 = nullptr;
     unsigned long long *d_Fscr64 = nullptr; /* scratch accumulators for mdrl_time_force */
@@ -92,6 +96,7 @@ struct mdrl_ctx {
     int kecap = 0;
     DevTotals *d_tot = nullptr;
     unsigned *d_err = nullptr;
+    int num_sms = 0;
 
     /* pair-eval staging */
     int pcap = 0;
@@ -235,15 +240,21 @@ static mdrl_status check_cells(mdrl_ctx *c) {
 static mdrl_status upload_tables(mdrl_ctx *c) {
     const int nidx = c->nseg * c->bins;
     const int nc = c->order + 1;
-    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4);
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr);
     auto coef = [&](int f, int k, int idx) { return c->tab[((size_t)f * nc + k) * nidx + idx]; };
     if (c->order == 1) {
         std::vector<float2> f2((size_t)3 * nidx), e2((size_t)3 * nidx);
-        for (int i = 0; i < nidx; ++i)
+        std::vector<float4> fr((size_t)2 * nidx);
+        for (int i = 0; i < nidx; ++i) {
             for (int f = 0; f < 3; ++f) {
                 f2[(size_t)3 * i + f] = make_float2(coef(f, 0, i), coef(f, 1, i));
                 e2[(size_t)3 * i + f] = make_float2(coef(3 + f, 0, i), coef(3 + f, 1, i));
             }
+            fr[(size_t)2 * i] = make_float4(coef(0, 0, i), coef(0, 1, i), coef(1, 0, i), coef(1, 1, i));
+            fr[(size_t)2 * i + 1] = make_float4(coef(2, 0, i), coef(2, 1, i), 0.0f, 0.0f);
+        }
+        MDRL_TRY(dalloc(&c->d_fr, fr.size()));
+        MDRL_CUDA(cudaMemcpy(c->d_fr, fr.data(), sizeof(float4) * fr.size(), cudaMemcpyHostToDevice));
         MDRL_TRY(dalloc(&c->d_f2, f2.size()));
         MDRL_TRY(dalloc(&c->d_e2, e2.size()));
         MDRL_CUDA(cudaMemcpy(c->d_f2, f2.data(), sizeof(float2) * f2.size(), cudaMemcpyHostToDevice));
@@ -278,7 +289,7 @@ static mdrl_status upload_tables(mdrl_ctx *c) {
 
 static TableDev table_dev(const mdrl_ctx *c) {
     TableDev t;
-    t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4;
+    t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4; t.fr = c->d_fr;
     t.order = c->order; t.nseg = c->nseg; t.bins = c->bins; t.lb = ilog2i(c->bins);
     t.min_log2 = c->min_log2;
     t.r2min = std::ldexp(1.0f, c->min_log2);
@@ -330,6 +341,7 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
     if (e == cudaSuccess) e = cudaEventCreate(&c->evf1);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_tot, sizeof(DevTotals));
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (e != cudaSuccess) {
         set_error(std::string("context setup: ") + cudaGetErrorString(e));
         mdrl_destroy(c);
@@ -344,7 +356,7 @@ static void free_particles(mdrl_ctx *c) {
     dfree(&c->d_ox); dfree(&c->d_oy); dfree(&c->d_oz);
     dfree(&c->d_ovx); dfree(&c->d_ovy); dfree(&c->d_ovz); dfree(&c->d_ocnt);
     for (int b = 0; b < 2; ++b) { dfree(&c->d_pos[b]); dfree(&c->d_vel[b]); dfree(&c->d_type[b]); dfree(&c->d_id[b]); }
-    dfree(&c->d_cell_of); dfree(&c->d_slot); dfree(&c->d_tmp); dfree(&c->d_sorted);
+    dfree(&c->d_cell_of); dfree(&c->d_slot); dfree(&c->d_tmp); dfree(&c->d_sorted); dfree(&c->d_key);
     dfree(&c->d_F64); dfree(&c->d_F32); dfree(&c->d_cnt);
     dfree(&c->d_Fscr64); dfree(&c->d_Fscr32);
     c->cap = 0;
@@ -359,7 +371,7 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
     free_particles(c);
-    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_pcoef);
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
     dfree(&c->d_tot); dfree(&c->d_err);
     dfree(&c->d_pr); dfree(&c->d_pn); dfree(&c->d_pout); dfree(&c->d_ptr); dfree(&c->d_ptn); dfree(&c->d_paux);
@@ -397,7 +409,7 @@ static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
         MDRL_TRY(dalloc(&c->d_type[b], m)); MDRL_TRY(dalloc(&c->d_id[b], m));
     }
     MDRL_TRY(dalloc(&c->d_cell_of, m)); MDRL_TRY(dalloc(&c->d_slot, m));
-    MDRL_TRY(dalloc(&c->d_tmp, m)); MDRL_TRY(dalloc(&c->d_sorted, m));
+    MDRL_TRY(dalloc(&c->d_tmp, m)); MDRL_TRY(dalloc(&c->d_sorted, m)); MDRL_TRY(dalloc(&c->d_key, m));
     if (c->p.accum == MDRL_ACC_FP32_ATOMIC) { MDRL_TRY(dalloc(&c->d_F32, 3 * m)); }
     else { MDRL_TRY(dalloc(&c->d_F64, 3 * m)); }
     MDRL_TRY(dalloc(&c->d_cnt, m));
@@ -428,23 +440,23 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
     /* the per-unit shift needs >= 4 cells on every axis; with 3 the per-pair wrap is used */
     const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
     force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap);
-    const size_t smem = force_smem_bytes(c->p.ntypes);
+    const size_t smem = force_smem_bytes(c->p.ntypes, extra);
+    /* The smem attribute is set once per kernel and device, on the first (uncaptured) launch. */
     {
-        /* The attribute is set once per kernel and device, outside any stream capture. */
         static std::mutex mu;
         static std::set<std::pair<const void *, int>> done;
         std::lock_guard<std::mutex> lock(mu);
         const std::pair<const void *, int> key((const void *)fn, c->p.device);
         if (!done.count(key)) {
             MDRL_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)force_smem_bytes(MDRL_MAX_TYPES)));
+                                           (int)force_smem_bytes(MDRL_MAX_TYPES, true)));
             done.insert(key);
         }
     }
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<units, kFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
-                                              c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit);
+                                         c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -456,19 +468,24 @@ static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
-/* Bin user-order arrays (already on the device) into the sorted buffers of slot `buf`. */
+
+
+/* Bin user-order arrays (already on the device) into the sorted buffers of slot `buf`.  With
+ * `spatial` the cells are ordered by Morton key (the force path's order), otherwise by index
+ * (the reference's in-cell order). */
 static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
-                            const float *q, const int *type, int buf) {
+                            const float *q, const int *type, int buf, bool spatial) {
     MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
     MDRL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
     if (n > 0) {
         k_bin_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, x, y, z, c->g, c->d_cell_of, c->d_slot,
-                                                        c->d_count, c->d_err);
+                                                        c->d_count, c->d_err, spatial ? c->d_key : nullptr);
     }
     k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
     if (n > 0) {
         k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
-        k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted);
+        k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted,
+                                                       spatial ? c->d_key : nullptr);
         k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, x, y, z, q, type, c->d_pos[buf],
                                                            c->d_type[buf], c->d_id[buf], c->d_F64,
                                                            c->d_F32, c->d_cnt, c->p.ntypes, c->d_err);
@@ -519,9 +536,10 @@ static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const floa
     const bool extra = counts != nullptr || (c->p.flags & MDRL_FLAG_ENERGY);
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
-    MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0));
+    MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0, true));
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
-    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, 0, c->d_kepart, c->d_tot);
+    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
+                                       extra ? 1 : 0);
     if (n > 0)
         k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, c->d_F32, c->d_cnt, fx, fy,
                                                       fz, counts);
@@ -593,7 +611,7 @@ extern "C" mdrl_status mdrl_bin(mdrl_ctx *c, int n, const float *x, const float 
         MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
         MDRL_CUDA(cudaMemcpyAsync(c->d_uz, z, fb, cudaMemcpyHostToDevice, c->stream));
     }
-    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, nullptr, nullptr, 0));
+    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, nullptr, nullptr, 0, false));
     if (cell_of && n > 0) MDRL_CUDA(cudaMemcpyAsync(cell_of, c->d_cell_of, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     if (cell_count) MDRL_CUDA(cudaMemcpyAsync(cell_count, c->d_count, sizeof(int) * c->ncells, cudaMemcpyDeviceToHost, c->stream));
     if (order && n > 0) MDRL_CUDA(cudaMemcpyAsync(order, c->d_sorted, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -733,14 +751,15 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
     }
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
     c->cur = 0;
-    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0));
+    MDRL_TRY(bin_user(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0, true));
     k_gather_vel<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], vx ? c->d_ovx : nullptr, c->d_ovy,
                                                       c->d_ovz, c->d_vel[0]);
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->mt_half, 0,
                                                 c->d_kepart);
-    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot);
+    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
+                                       extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_TRY(check_device_errors(c));
@@ -759,19 +778,21 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
     k_kick_drift_bin<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pos[a], c->d_vel[a], c->d_type[a], c->d_F64,
                                                           c->d_F32, mt, dt, c->g, c->d_cell_of, c->d_slot,
-                                                          c->d_count);
+                                                          c->d_count, c->d_key);
     k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
     k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
-    k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted);
+    k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key);
     k_gather_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, c->d_pos[a], c->d_vel[a], c->d_type[a],
                                                         c->d_id[a], c->d_pos[b], c->d_vel[b], c->d_type[b],
                                                         c->d_id[b], c->d_F64, c->d_F32);
     if (extra) MDRL_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * (size_t)n, c->stream));
     MDRL_TRY(launch_force(c, n, c->d_pos[b], c->d_type[b], extra));
-    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->mt_half,
-                                                vv ? 1 : 0, c->d_kepart);
-    k_totals<<<1, 256, 0, c->stream>>>(c->ncells * kHalfShellCells, c->d_unit, nblk(n, 256), c->d_kepart,
-                                       c->d_tot);
+    /* kinetic energy only when energies are requested */
+    if (vv || extra)
+        k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->mt_half,
+                                                    vv ? 1 : 0, extra ? c->d_kepart : nullptr);
+    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
+                                       c->d_kepart, c->d_tot, extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
 }

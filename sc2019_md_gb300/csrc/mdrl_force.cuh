@@ -23,6 +23,10 @@
  * rule, hence the same r2 bit for bit.  With 3 cells on an axis the per-pair rule is kept
  * (WRAP = true).
  *
+ * Within a cell the particles are in Morton order of their position inside the cell, so the 4 i
+ * x 8 j candidates of one warp instruction are spatially coherent: for ~70 % of them no lane
+ * passes the filter and the warp skips the force path; the busy ones carry ~14 accepted lanes.
+ *
  * Table address.  r2e = max(r2, 2^min_log2); (bits(r2e) >> (23 - log2 bins)) - ((127 +
  * min_log2) << log2 bins) is segment * bins + bin, the address the RTL forms from the exponent
  * and the top mantissa bits (SC/RL_LJ_Evaluate_Pairs_1st_Order.v:179-193).  Accepted pairs have
@@ -34,24 +38,31 @@
 
 namespace mdrl {
 
-constexpr int kFW = 4;                 /* warps per force CTA */
+#ifndef MDRL_FORCE_WARPS
+#define MDRL_FORCE_WARPS 4
+#endif
+constexpr int kFW = MDRL_FORCE_WARPS;  /* warps per force CTA */
 constexpr int kFT = kFW * 32;
 constexpr int kStepsPerPiece = 6;      /* j-steps (of 8 particles) per piece */
 
 typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
                          int, float, int, unsigned long long *, float *, int *, UnitOut *);
 
+/* Work items (one per unit): the result slots k_totals sums. */
+inline int force_items(int ncells) { return ncells * kHalfShellCells; }
+
 force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap);
 
-inline size_t force_smem_bytes(int ntypes) {
+inline size_t force_smem_bytes(int ntypes, bool extra) {
     return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
-           sizeof(float) * kFW * 6 * kChunk + sizeof(int) * kFW * 2 * kChunk;
+           sizeof(float) * kFW * 6 * kChunk + (extra ? sizeof(int) * kFW * 2 * kChunk : 0);
 }
 
+/* The pair functions of an accepted pair at r2e = max(r2, 2^min_log2).  Order 1 reads one
+ * 32-byte row {c0_14, c1_14, c0_8, c1_8}{c0_3, c1_3, 0, 0}; orders 2-3 read float4 rows. */
 template <int ORDER, bool SEP, bool ENERGY>
-__device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2, bool coul,
-                                                    float &v14, float &v8, float &v3, float &v12,
-                                                    float &v6, float &v1) {
+__device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2, bool coul, float &v14,
+                                                    float &v8, float &v3, float &v12, float &v6, float &v1) {
     if (ORDER == 0) {
         int below;
         pair_functions<0, SEP, ENERGY>(t, r2, coul, v14, v8, v3, v12, v6, v1, below);
@@ -60,17 +71,17 @@ __device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2,
     const float r2e = fmaxf(r2, t.r2min);
     const int idx = (int)(__float_as_uint(r2e) >> (23 - t.lb)) - ((127 + t.min_log2) << t.lb);
     if (ORDER == 1) {
-        const float2 a = __ldg(t.f2 + 3 * idx), b = __ldg(t.f2 + 3 * idx + 1);
+        const float4 a = __ldg(t.fr + 2 * idx);
         v14 = madd<SEP>(a.y, r2e, a.x);
-        v8 = madd<SEP>(b.y, r2e, b.x);
+        v8 = madd<SEP>(a.w, r2e, a.z);
         v3 = 0.0f;
-        if (coul) { const float2 c = __ldg(t.f2 + 3 * idx + 2); v3 = madd<SEP>(c.y, r2e, c.x); }
+        if (coul) { const float4 c = __ldg(t.fr + 2 * idx + 1); v3 = madd<SEP>(c.y, r2e, c.x); }
         if (ENERGY) {
             const float2 d = __ldg(t.e2 + 3 * idx), e = __ldg(t.e2 + 3 * idx + 1);
             v12 = madd<SEP>(d.y, r2e, d.x);
             v6 = madd<SEP>(e.y, r2e, e.x);
             v1 = 0.0f;
-            if (coul) { const float2 g = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(g.y, r2e, g.x); }
+            if (coul) { const float2 gg = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(gg.y, r2e, gg.x); }
         }
     } else {
         v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), r2e);
@@ -148,7 +159,7 @@ __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32,
 }
 
 template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP>
-__global__ void __launch_bounds__(kFT, 4)
+__global__ void __launch_bounds__(kFT, 16 / kFW)
 k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         const int *__restrict__ cstart, Geom g, TableDev tab, const float4 *__restrict__ pcoef,
         int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
@@ -183,7 +194,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
     const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
     const bool coul = ke != 0.0f;
-    const float nan = __int_as_float(0x7fc00000);
+    const float far = 1.0e18f;   /* padding lanes: finite, so r2 ~ 3e36 > rc2 */
     float *wFi = sF + warp * 6 * kChunk;
     float *wFj = wFi + 3 * kChunk;
     int *wCi = sC + warp * 2 * kChunk;
@@ -241,7 +252,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                         qi[k] = __fmul_rn(ke, pp.w);
                         tti[k] = sIt[il];
                     } else {
-                        xi[k] = nan; yi[k] = nan; zi[k] = nan; qi[k] = 0.0f; tti[k] = 0;
+                        xi[k] = far; yi[k] = far; zi[k] = far; qi[k] = 0.0f; tti[k] = 0;
                     }
                 }
                 float fi[24];
@@ -250,7 +261,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                 int ci[8] = {0, 0, 0, 0, 0, 0, 0, 0};
                 for (int s = s0; s < s1; ++s) {
                     const int jl = s * 8 + col;
-                    float xj = nan, yj = nan, zj = nan, qj = 0.0f;
+                    float xj = -far, yj = -far, zj = -far, qj = 0.0f;
                     int ttj = 0;
                     if (jl < nj) {
                         const float4 pp = sJp[jl];
@@ -259,6 +270,29 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                     }
                     float fjx = 0.f, fjy = 0.f, fjz = 0.f;
                     int cj = 0;
+#ifdef MDRL_FORCE_SPLIT
+                    /* filter phase: 8 independent r2 chains; force phase only for accepted pairs
+                     * (the differences are recomputed there with the same two roundings) */
+                    float r2k[8];
+                    unsigned okm = 0;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
+                        const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
+                        const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                        r2k[k] = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        bool ok = (r2k[k] > 0.0f) && (r2k[k] <= g.rc2);
+                        if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
+                        okm |= ok ? (1u << k) : 0u;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        if (okm & (1u << k)) {
+                            const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
+                            const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
+                            const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                            const float r2 = r2k[k];
+#else
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
@@ -269,6 +303,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                         bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
                         if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
                         if (ok) {
+#endif
                             float v14, v8, v3, v12, v6, v1;
                             pair_functions_fast<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1);
                             const float4 pc = sCoef[tti[k] + ttj];

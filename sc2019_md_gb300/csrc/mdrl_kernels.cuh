@@ -32,6 +32,8 @@ namespace mdrl {
 struct TableDev {
     const float2 *f2, *e2;
     const float4 *f4, *e4;
+    const float4 *fr;   /* order 1, force functions packed per index in one 32-byte sector:
+                           {c0_14, c1_14, c0_8, c1_8}, {c0_3, c1_3, 0, 0} */
     int order, nseg, bins, lb, min_log2;
     float r2min;
 };
@@ -169,22 +171,61 @@ __device__ __forceinline__ int cell_of_pos(const Geom &g, float x, float y, floa
     return (cx * g.nc[1] + cy) * g.nc[2] + cz;
 }
 
+/* 30-bit Morton code of a position inside its cell (10 bits per axis): the in-cell sort key of
+ * the force path.  Only an ordering, so its rounding does not matter; ties break on the index. */
+__device__ __forceinline__ unsigned spread10(unsigned v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ unsigned cell_morton(const Geom &g, float x, float y, float z, int c) {
+    const int cz = c % g.nc[2], cy = (c / g.nc[2]) % g.nc[1], cx = c / (g.nc[1] * g.nc[2]);
+    const float p[3] = {x, y, z};
+    const int cc[3] = {cx, cy, cz};
+    unsigned q[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float loc = (p[d] - (float)cc[d] * g.edge[d]) * (1024.0f / g.edge[d]);
+        q[d] = (unsigned)min(1023, max(0, (int)loc));
+    }
+    return (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+}
+
 __device__ __forceinline__ bool in_box(const Geom &g, float x, float y, float z) {
     return x >= 0.0f && x < g.L[0] && y >= 0.0f && y < g.L[1] && z >= 0.0f && z < g.L[2];
+}
+
+/* Arrival slot of a particle in cell c: lanes of a warp that share c take consecutive slots with
+ * one atomic per distinct cell (cell-sorted particles mostly share cells within a warp). */
+__device__ __forceinline__ int cell_slot(int *count, int c) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, c);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count + c, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + rank;
 }
 
 /* Cell of each user-order particle, with its arrival slot in the cell. */
 static __global__ void k_bin_user(int n, const float *__restrict__ x, const float *__restrict__ y,
                            const float *__restrict__ z, Geom g, int *__restrict__ cell_of,
                            int *__restrict__ slot, int *__restrict__ count,
-                           unsigned *__restrict__ err) {
+                           unsigned *__restrict__ err, unsigned *__restrict__ key) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float px = x[i], py = y[i], pz = z[i];
     if (!in_box(g, px, py, pz)) atomicOr(err, kErrPosition);
     const int c = cell_of_pos(g, px, py, pz);
     cell_of[i] = c;
-    slot[i] = atomicAdd(count + c, 1);
+    if (key) key[i] = cell_morton(g, px, py, pz, c);
+    slot[i] = cell_slot(count, c);
 }
 
 /* Exclusive scan of the cell counts (one CTA), plus the largest occupancy. */
@@ -220,25 +261,36 @@ static __global__ void k_scatter(int n, const int *__restrict__ cell_of, const i
     tmp[start[cell_of[i]] + slot[i]] = i;
 }
 
-/* Order each cell's ids ascending: the rank of an id is the number of smaller ids in its cell. */
+/* Order each cell's particles: by index (the reference's in-cell order, input order), or, when
+ * key is given, by (key, index).  The rank of an element is the number of smaller ones. */
 static __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start,
-                                                   const int *__restrict__ tmp,
-                                                   int *__restrict__ sorted) {
-    __shared__ int s_ids[1024];
+                                                          const int *__restrict__ tmp,
+                                                          int *__restrict__ sorted,
+                                                          const unsigned *__restrict__ key) {
+    __shared__ unsigned long long s_k[1024];
     const int c = blockIdx.x;
     const int s = start[c], m = start[c + 1] - s;
     if (m == 0) return;
     const bool staged = m <= 1024;
     if (staged) {
-        for (int e = threadIdx.x; e < m; e += blockDim.x) s_ids[e] = tmp[s + e];
+        for (int e = threadIdx.x; e < m; e += blockDim.x) {
+            const int id = tmp[s + e];
+            s_k[e] = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id;
+        }
         __syncthreads();
     }
-    const int *ids = staged ? s_ids : tmp + s;
     for (int e = threadIdx.x; e < m; e += blockDim.x) {
-        const int id = ids[e];
+        unsigned long long me;
+        if (staged) me = s_k[e];
+        else { const int id = tmp[s + e]; me = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id; }
         int r = 0;
-        for (int q = 0; q < m; ++q) r += ids[q] < id;
-        sorted[s + r] = id;
+        for (int q = 0; q < m; ++q) {
+            unsigned long long o;
+            if (staged) o = s_k[q];
+            else { const int id = tmp[s + q]; o = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id; }
+            r += o < me;
+        }
+        sorted[s + r] = (int)(me & 0xffffffffu);
     }
 }
 
@@ -263,18 +315,22 @@ static __global__ void k_gather_user(int n, const int *__restrict__ sorted, cons
     if (counts) counts[k] = 0;
 }
 
-/* Totals over units and kinetic-energy partials, in a fixed order (one CTA). */
+/* Totals over units and kinetic-energy partials, in a fixed order (one CTA).  GB300 runs FP64 at
+ * a small fraction of its FP32 rate, so the FP64 energy sums run only when energies were computed. */
 static __global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__restrict__ uout,
-                                                int nke, const double *__restrict__ kepart,
-                                                DevTotals *tot) {
+                                                       int nke, const double *__restrict__ kepart,
+                                                       DevTotals *tot, int with_energy) {
     __shared__ double s_d[256][4];
     __shared__ unsigned long long s_u[256][2];
     const int t = threadIdx.x;
     double a = 0, b = 0, c = 0, k = 0;
     unsigned long long p = 0, q = 0;
     for (int u = t; u < nunits; u += 256) {
-        a += uout[u].e_lj; b += uout[u].e_coul; c += uout[u].virial;
-        p += uout[u].pairs; q += uout[u].below;
+        p += uout[u].pairs;
+        if (with_energy) {
+            a += uout[u].e_lj; b += uout[u].e_coul; c += uout[u].virial;
+            q += uout[u].below;
+        }
     }
     for (int u = t; u < nke; u += 256) k += kepart[u];
     s_d[t][0] = a; s_d[t][1] = b; s_d[t][2] = c; s_d[t][3] = k;
@@ -282,7 +338,8 @@ static __global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut
     __syncthreads();
     for (int off = 128; off > 0; off >>= 1) {
         if (t < off) {
-            for (int m = 0; m < 4; ++m) s_d[t][m] += s_d[t + off][m];
+            if (with_energy || nke > 0)
+                for (int m = 0; m < 4; ++m) s_d[t][m] += s_d[t + off][m];
             s_u[t][0] += s_u[t + off][0];
             s_u[t][1] += s_u[t + off][1];
         }
@@ -336,7 +393,7 @@ static __global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 
                                  const unsigned long long *__restrict__ F64,
                                  const float *__restrict__ F32, MassTab mt, float dt, Geom g,
                                  int *__restrict__ cell_of, int *__restrict__ slot,
-                                 int *__restrict__ count) {
+                                 int *__restrict__ count, unsigned *__restrict__ key) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const float cm = mt.cm[ptype[k]];
@@ -352,7 +409,8 @@ static __global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 
     pos[k] = p;
     const int c = cell_of_pos(g, p.x, p.y, p.z);
     cell_of[k] = c;
-    slot[k] = atomicAdd(count + c, 1);
+    key[k] = cell_morton(g, p.x, p.y, p.z, c);
+    slot[k] = cell_slot(count, c);
 }
 
 /* Reorder the state into the new cell order and clear the force accumulators. */
@@ -373,14 +431,15 @@ static __global__ void k_gather_state(int n, const int *__restrict__ sorted,
     if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
 }
 
-/* Second half kick (velocity Verlet) and per-block kinetic energy partials. */
+/* Second half kick (velocity Verlet) and, when asked, per-block kinetic-energy partials
+ * (FP32 per particle and within the block, in a fixed order; FP64 across blocks). */
 static __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, const int *__restrict__ ptype,
-                                              const unsigned long long *__restrict__ F64,
-                                              const float *__restrict__ F32, MassTab mt, int do_kick,
-                                              double *__restrict__ kepart) {
-    __shared__ double s_k[256];
+                                                     const unsigned long long *__restrict__ F64,
+                                                     const float *__restrict__ F32, MassTab mt, int do_kick,
+                                                     double *__restrict__ kepart) {
+    __shared__ float s_k[8];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    double ke = 0.0;
+    float ke = 0.0f;
     if (k < n) {
         const int t = ptype[k];
         float4 v = vel[k];
@@ -392,16 +451,18 @@ static __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__
             vel[k] = v;
         }
         /* 1/2 m v^2 in kcal/mol with v in A/fs and m in amu: divide by 4.184e-4. */
-        ke = 0.5 * (double)mt.mass[t] *
-             ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z) / 4.184e-4;
+        if (kepart) ke = 0.5f * mt.mass[t] * (v.x * v.x + v.y * v.y + v.z * v.z) * (1.0f / 4.184e-4f);
     }
-    s_k[threadIdx.x] = ke;
+    if (!kepart) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+    if ((threadIdx.x & 31) == 0) s_k[threadIdx.x >> 5] = ke;
     __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
-        if (threadIdx.x < off) s_k[threadIdx.x] += s_k[threadIdx.x + off];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += s_k[w];
+        kepart[blockIdx.x] = b;
     }
-    if (threadIdx.x == 0) kepart[blockIdx.x] = s_k[0];
 }
 
 /* Sorted state back to user order. */

@@ -8,13 +8,13 @@
  * state exactly as it found it.  mdrl_force_eval needs a context (mdrl_create), and a context
  * allocates its buffers; this entry point needs none.
  *
- * How: all scratch of the path — cell counts and starts, the stable in-cell order, the
+ * How: all scratch of the path — cell counts and starts, the in-cell order and its keys, the
  * cell-sorted copy of the particles, the int64 force accumulators, the per-unit reduction slots
  * and the tables — lives in one file-scope static __device__ array of kStaticBytes (16 MiB),
  * which every GPU that loads the library holds until the process exits.  The caller passes
  * device pointers to its inputs and outputs and a stream.
  *
- * Limits: n <= 131,072 particles, <= 8,192 cells, nseg * bins <= 16,384 table entries, int64
+ * Limits: n <= 131,072 particles, <= 4,096 cells, nseg * bins <= 16,384 table entries, int64
  * fixed-point accumulation only; larger requests are rejected with MDRL_ERR_RANGE and a message.
  *
  * Set-up: the first call on a device (with that device current) looks up the device address of
@@ -38,7 +38,7 @@
 namespace mdrl {
 
 constexpr int kStaticMaxN = 131072;
-constexpr int kStaticMaxCells = 8192;
+constexpr int kStaticMaxCells = 4096;
 constexpr int kStaticMaxTable = 16384;
 constexpr size_t kStaticBytes = size_t(16) << 20;
 constexpr int kStaticMaxDevices = 64;
@@ -51,8 +51,8 @@ constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 /* Byte offsets of the sub-buffers inside the array. */
 struct Layout {
-    size_t err, tot, count, start, unit, cell_of, slot, tmp, sorted, pos, type, id, F64, tabf, tabe,
-        pcoef, end;
+    size_t err, tot, count, start, unit, cell_of, slot, tmp, sorted, key, pos, type, id, F64, tabf,
+        tabe, tabr, pcoef, end;
 };
 
 constexpr Layout make_layout() {
@@ -67,12 +67,14 @@ constexpr Layout make_layout() {
     l.slot = o;    o = align256(o + sizeof(int) * kStaticMaxN);
     l.tmp = o;     o = align256(o + sizeof(int) * kStaticMaxN);
     l.sorted = o;  o = align256(o + sizeof(int) * kStaticMaxN);
+    l.key = o;     o = align256(o + sizeof(unsigned) * kStaticMaxN);
     l.pos = o;     o = align256(o + sizeof(float4) * kStaticMaxN);
     l.type = o;    o = align256(o + sizeof(int) * kStaticMaxN);
     l.id = o;      o = align256(o + sizeof(int) * kStaticMaxN);
     l.F64 = o;     o = align256(o + sizeof(unsigned long long) * 3 * kStaticMaxN);
     l.tabf = o;    o = align256(o + sizeof(float4) * 3 * kStaticMaxTable);
     l.tabe = o;    o = align256(o + sizeof(float4) * 3 * kStaticMaxTable);
+    l.tabr = o;    o = align256(o + sizeof(float4) * 2 * kStaticMaxTable);
     l.pcoef = o;   o = align256(o + sizeof(float4) * MDRL_MAX_TYPES * MDRL_MAX_TYPES);
     l.end = o;
     return l;
@@ -182,6 +184,7 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     int *d_slot = (int *)(b + kLayout.slot);
     int *d_tmp = (int *)(b + kLayout.tmp);
     int *d_sorted = (int *)(b + kLayout.sorted);
+    unsigned *d_key = (unsigned *)(b + kLayout.key);
     float4 *d_pos = (float4 *)(b + kLayout.pos);
     int *d_type = (int *)(b + kLayout.type);
     int *d_id = (int *)(b + kLayout.id);
@@ -202,11 +205,16 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
         auto coef = [&](int f, int k, int i) { return tab[((size_t)f * nc + k) * nidx + i]; };
         if (order == 1) {
             std::vector<float2> f2((size_t)3 * nidx), e2((size_t)3 * nidx);
-            for (int i = 0; i < nidx; ++i)
+            std::vector<float4> fr((size_t)2 * nidx);
+            for (int i = 0; i < nidx; ++i) {
                 for (int f = 0; f < 3; ++f) {
                     f2[(size_t)3 * i + f] = make_float2(coef(f, 0, i), coef(f, 1, i));
                     e2[(size_t)3 * i + f] = make_float2(coef(3 + f, 0, i), coef(3 + f, 1, i));
                 }
+                fr[(size_t)2 * i] = make_float4(coef(0, 0, i), coef(0, 1, i), coef(1, 0, i), coef(1, 1, i));
+                fr[(size_t)2 * i + 1] = make_float4(coef(2, 0, i), coef(2, 1, i), 0.0f, 0.0f);
+            }
+            ST_CUDA(cudaMemcpyAsync(b + kLayout.tabr, fr.data(), sizeof(float4) * fr.size(), cudaMemcpyHostToDevice, st));
             ST_CUDA(cudaMemcpyAsync(b + kLayout.tabf, f2.data(), sizeof(float2) * f2.size(), cudaMemcpyHostToDevice, st));
             ST_CUDA(cudaMemcpyAsync(b + kLayout.tabe, e2.data(), sizeof(float2) * e2.size(), cudaMemcpyHostToDevice, st));
         } else {
@@ -233,6 +241,7 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     TableDev tab;
     tab.f2 = (const float2 *)(b + kLayout.tabf); tab.e2 = (const float2 *)(b + kLayout.tabe);
     tab.f4 = (const float4 *)(b + kLayout.tabf); tab.e4 = (const float4 *)(b + kLayout.tabe);
+    tab.fr = (const float4 *)(b + kLayout.tabr);
     tab.order = order; tab.nseg = nseg; tab.bins = bins;
     int lb = 0;
     while ((1 << lb) < bins) ++lb;
@@ -244,23 +253,23 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     ST_CUDA(cudaMemsetAsync(d_tot, 0, sizeof(DevTotals), st));
     ST_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * nc, st));
     const int blk = 256, grid = (n + blk - 1) / blk;
-    if (n > 0) k_bin_user<<<grid, blk, 0, st>>>(n, x, y, z, g, d_cell_of, d_slot, d_count, d_err);
+    if (n > 0) k_bin_user<<<grid, blk, 0, st>>>(n, x, y, z, g, d_cell_of, d_slot, d_count, d_err, d_key);
     k_scan<<<1, 1024, 0, st>>>(nc, d_count, d_start, d_tot);
     if (n > 0) {
         k_scatter<<<grid, blk, 0, st>>>(n, d_cell_of, d_slot, d_start, d_tmp);
-        k_cell_sort<<<nc, 128, 0, st>>>(d_start, d_tmp, d_sorted);
+        k_cell_sort<<<nc, 128, 0, st>>>(d_start, d_tmp, d_sorted, d_key);
         k_gather_user<<<grid, blk, 0, st>>>(n, d_sorted, x, y, z, q, type, d_pos, d_type, d_id, d_F64, nullptr,
                                             nullptr, p->ntypes, d_err);
     }
     const bool wrap = g.nc[0] < 4 || g.nc[1] < 4 || g.nc[2] < 4;
     const int ord = p->eval == MDRL_EVAL_DIRECT ? 0 : order;
     force_fn fn = pick_force(ord, p->arith == MDRL_ARITH_SEPARATE, false, MDRL_ACC_FIXED64, wrap);
-    const size_t smem = force_smem_bytes(p->ntypes);
+    const size_t smem = force_smem_bytes(p->ntypes, false);
     ST_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)force_smem_bytes(MDRL_MAX_TYPES)));
+                                 (int)force_smem_bytes(MDRL_MAX_TYPES, true)));
     fn<<<nc * kHalfShellCells, kFT, smem, st>>>(d_pos, d_type, d_start, g, tab, d_pcoef, p->ntypes,
                                                 (float)p->coulomb_k, n, d_F64, nullptr, nullptr, d_unit);
-    k_totals<<<1, 256, 0, st>>>(nc * kHalfShellCells, d_unit, 0, nullptr, d_tot);
+    k_totals<<<1, 256, 0, st>>>(force_items(nc), d_unit, 0, nullptr, d_tot, 0);
     if (n > 0)
         k_unsort<<<grid, blk, 0, st>>>(n, d_id, d_F64, nullptr, nullptr, fx, fy, fz, nullptr);
     ST_CUDA(cudaGetLastError());

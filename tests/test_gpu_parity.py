@@ -127,10 +127,12 @@ def test_force_lj1728_and_fp64_error():
     assert emax <= 2e-5, emax
 
 
-def test_force_ljc_fp64_error_1024_bins():
-    """LJ+Coulomb, 4 types: median per-particle relative error against FP64 direct <= 1e-5."""
+@pytest.mark.parametrize("bins", [512, 1024])
+def test_force_ljc_fp64_error(bins):
+    """LJ+Coulomb, 4 types: median per-particle relative error against FP64 direct <= 1e-5 with
+    1st-order 512- and 1024-bin tables (the benchmark's setting is 512)."""
     sysm = systems.small_ljc(6000, 49.6, 12.0, seed=5)
-    p = sysm.params(table_bins=1024)
+    p = sysm.params(table_bins=bins)
     with m.Context(p) as ctx:
         F, st, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
         o = oracle_from_ctx(ctx, sysm)

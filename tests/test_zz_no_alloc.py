@@ -55,4 +55,4 @@ def test_static_entry_point_rejects_sizes_beyond_its_limit():
     big = s.params(box=(400.0, 400.0, 400.0), ncell=(33, 33, 33))   # 35,937 cells
     with pytest.raises(m.MdrlError) as e:
         m.force_eval_static(big, 10, 1, 1, 1, None, None, 1, 1, 1, None)
-    assert e.value.status == 3 and "8192" in str(e.value)
+    assert e.value.status == 3 and "4096" in str(e.value)
