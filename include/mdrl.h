@@ -49,7 +49,8 @@ enum {
     MDRL_ACC_FIXED64 = 0,   /* FP32 partial sums in a fixed traversal order, int64 2^-24 atomics:
                                bit-reproducible run to run */
     MDRL_ACC_FP32_ATOMIC = 1, /* FP32 atomics ("plain"): order-dependent rounding */
-    MDRL_ACC_KAHAN = 2      /* compensated FP32 partial sums, then int64 fixed point */
+    MDRL_ACC_KAHAN = 2      /* FP32 partial sums in a fixed order, then a compensated FP32 global
+                               sum (high + low planes, TwoSum error of every atomic) */
 };
 
 /* Per-pair arithmetic. */

@@ -410,8 +410,8 @@ static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
     }
     MDRL_TRY(dalloc(&c->d_cell_of, m)); MDRL_TRY(dalloc(&c->d_slot, m));
     MDRL_TRY(dalloc(&c->d_tmp, m)); MDRL_TRY(dalloc(&c->d_sorted, m)); MDRL_TRY(dalloc(&c->d_key, m));
-    if (c->p.accum == MDRL_ACC_FP32_ATOMIC) { MDRL_TRY(dalloc(&c->d_F32, 3 * m)); }
-    else { MDRL_TRY(dalloc(&c->d_F64, 3 * m)); }
+    if (c->p.accum == MDRL_ACC_FIXED64) { MDRL_TRY(dalloc(&c->d_F64, 3 * m)); }
+    else { MDRL_TRY(dalloc(&c->d_F32, 6 * m)); }   /* high and low planes */
     MDRL_TRY(dalloc(&c->d_cnt, m));
     const int nke = (n + 255) / 256;
     MDRL_TRY(dalloc(&c->d_kepart, nke));
@@ -427,9 +427,11 @@ static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
 namespace mdrl {
 force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap);
 force_fn pick_force_acc1(int order, bool sep, bool extra, bool wrap);
+force_fn pick_force_acc2(int order, bool sep, bool extra, bool wrap);
 force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap) {
-    return acc == MDRL_ACC_FP32_ATOMIC ? pick_force_acc1(order, sep, extra, wrap)
-                                       : pick_force_acc0(order, sep, extra, wrap);
+    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_acc1(order, sep, extra, wrap);
+    if (acc == MDRL_ACC_KAHAN) return pick_force_acc2(order, sep, extra, wrap);
+    return pick_force_acc0(order, sep, extra, wrap);
 }
 }  // namespace mdrl
 
@@ -841,10 +843,10 @@ extern "C" mdrl_status mdrl_time_force(mdrl_ctx *c, float *ms) {
     if (!c->have_state) { set_error("mdrl_time_force: call mdrl_set_state first"); return MDRL_ERR_STATE; }
     MDRL_CUDA(cudaSetDevice(c->p.device));
     const int n = c->n, a = c->cur;
-    const bool fp32 = c->p.accum == MDRL_ACC_FP32_ATOMIC;
-    if (fp32 && !c->d_Fscr32) MDRL_TRY(dalloc(&c->d_Fscr32, 3 * (size_t)c->cap));
+    const bool fp32 = c->p.accum != MDRL_ACC_FIXED64;
+    if (fp32 && !c->d_Fscr32) MDRL_TRY(dalloc(&c->d_Fscr32, 6 * (size_t)c->cap));
     if (!fp32 && !c->d_Fscr64) MDRL_TRY(dalloc(&c->d_Fscr64, 3 * (size_t)c->cap));
-    if (fp32) MDRL_CUDA(cudaMemsetAsync(c->d_Fscr32, 0, sizeof(float) * 3 * (size_t)n, c->stream));
+    if (fp32) MDRL_CUDA(cudaMemsetAsync(c->d_Fscr32, 0, sizeof(float) * 6 * (size_t)n, c->stream));
     else MDRL_CUDA(cudaMemsetAsync(c->d_Fscr64, 0, sizeof(unsigned long long) * 3 * (size_t)n, c->stream));
     MDRL_TRY(launch_force_into(c, n, c->d_pos[a], c->d_type[a], false, c->d_Fscr64, c->d_Fscr32));
     MDRL_CUDA(cudaStreamSynchronize(c->stream));

@@ -144,6 +144,17 @@ __device__ __forceinline__ int reduce_scatter8i(int (&v)[8], int col) {
     return keep + __shfl_xor_sync(0xffffffffu, send, 1);
 }
 
+/* Compensated FP32 accumulation: add v to the high plane with an atomic that returns the old
+ * value, recompute the rounded sum and add its exact rounding error (Knuth's TwoSum) to the low
+ * plane.  high + low then carries the global sum to ~FP32^2 relative error. */
+__device__ __forceinline__ void kahan_add(float *hi, float *lo, float v) {
+    const float old = atomicAdd(hi, v);
+    const float s = __fadd_rn(old, v);
+    const float bb = __fsub_rn(s, old);
+    const float e = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    if (e != 0.0f) atomicAdd(lo, e);
+}
+
 template <int ACC>
 __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32, int n, int g, float fx,
                                             float fy, float fz) {
@@ -151,6 +162,10 @@ __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32,
         atomicAdd(F32 + g, fx);
         atomicAdd(F32 + n + g, fy);
         atomicAdd(F32 + 2 * n + g, fz);
+    } else if (ACC == 2) {
+        kahan_add(F32 + g, F32 + 3 * (size_t)n + g, fx);
+        kahan_add(F32 + n + g, F32 + 4 * (size_t)n + g, fy);
+        kahan_add(F32 + 2 * n + g, F32 + 5 * (size_t)n + g, fz);
     } else {
         atomicAdd(F64 + g, to_fixed(fx));
         atomicAdd(F64 + n + g, to_fixed(fy));

@@ -311,7 +311,10 @@ static __global__ void k_gather_user(int n, const int *__restrict__ sorted, cons
     ptype[k] = t;
     pid[k] = id;
     if (F64) { F64[k] = 0ull; F64[n + k] = 0ull; F64[2 * n + k] = 0ull; }
-    if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
+    if (F32) {
+#pragma unroll
+        for (int d = 0; d < 6; ++d) F32[(size_t)d * n + k] = 0.0f;   /* hi planes 0-2, lo planes 3-5 */
+    }
     if (counts) counts[k] = 0;
 }
 
@@ -364,7 +367,9 @@ static __global__ void k_unsort(int n, const int *__restrict__ pid, const unsign
     if (F64) {
         fx[id] = from_fixed(F64[k]); fy[id] = from_fixed(F64[n + k]); fz[id] = from_fixed(F64[2 * n + k]);
     } else {
-        fx[id] = F32[k]; fy[id] = F32[n + k]; fz[id] = F32[2 * n + k];
+        fx[id] = F32[k] + F32[3 * (size_t)n + k];
+        fy[id] = F32[n + k] + F32[4 * (size_t)n + k];
+        fz[id] = F32[2 * n + k] + F32[5 * (size_t)n + k];
     }
     if (cnt_u) cnt_u[id] = cnt_s[k];
 }
@@ -384,7 +389,9 @@ __device__ __forceinline__ float wrap_pos(float x, float L) {
 
 __device__ __forceinline__ float force_of(const unsigned long long *F64, const float *F32, int n,
                                           int k, int d) {
-    return F64 ? from_fixed(F64[(size_t)d * n + k]) : F32[(size_t)d * n + k];
+    /* FP32 accumulation keeps a high and a low (compensation) plane; the low one is zero in
+     * the plain FP32-atomic mode */
+    return F64 ? from_fixed(F64[(size_t)d * n + k]) : F32[(size_t)d * n + k] + F32[(size_t)(d + 3) * n + k];
 }
 
 /* v += F * cm[type] (half or full kick), x += v * dt, wrap, and bin the new position. */
@@ -428,7 +435,10 @@ static __global__ void k_gather_state(int n, const int *__restrict__ sorted,
     type1[k] = type0[o];
     id1[k] = id0[o];
     if (F64) { F64[k] = 0ull; F64[n + k] = 0ull; F64[2 * n + k] = 0ull; }
-    if (F32) { F32[k] = 0.0f; F32[n + k] = 0.0f; F32[2 * n + k] = 0.0f; }
+    if (F32) {
+#pragma unroll
+        for (int d = 0; d < 6; ++d) F32[(size_t)d * n + k] = 0.0f;   /* hi planes 0-2, lo planes 3-5 */
+    }
 }
 
 /* Second half kick (velocity Verlet) and, when asked, per-block kinetic-energy partials

@@ -11,7 +11,8 @@ Workloads (all periodic):
               (sigma 2.0-3.8, eps 0.02-0.2, Lorentz-Berthelot), charges +-0.42 e net neutral,
               uniform placement at 0.1 /A^3 with 1.0 A minimum separation.
   ljc1m       1,048,576 atoms in a 224 A cube, rc 10 (22^3 cells), 16 types, charges U(-0.8, 0.8)
-              shifted to net zero.
+              shifted to net zero; 1.0 A minimum separation as for ljc92k (without one, random
+              overlaps give pair forces beyond the int64 fixed-point range).
 """
 from __future__ import annotations
 
@@ -122,7 +123,7 @@ def ljc92k(n: int = 92224, box=(108.86, 108.86, 77.76), seed_offset: int = 0) ->
 
 def ljc1m(n: int = 1048576, L: float = 224.0, seed_offset: int = 0) -> System:
     rng = np.random.default_rng(20191117 + 5 + seed_offset)
-    pos = wrap_into_box(rng.random((n, 3)) * L, (L, L, L))
+    pos = wrap_into_box(uniform_min_sep(n, (L, L, L), 1.0, rng), (L, L, L))
     T = 16
     sigma = list(rng.uniform(2.5, 3.8, T))
     eps = list(rng.uniform(0.05, 0.25, T))

@@ -147,6 +147,14 @@ def test_force_fp32_atomic_plain():
     _check_force(sysm, p, tol=1e-5)
 
 
+def test_force_kahan_compensated():
+    """Compensated FP32 accumulation: FP32 partial sums in a fixed order plus a TwoSum-compensated
+    global sum -- within the FP32 summation bound of the oracle's exact sum."""
+    sysm = systems.small_ljc(3000, 37.5, 12.0, seed=23)
+    p = sysm.params(accum=m.ACC_KAHAN, table_bins=512)
+    _check_force(sysm, p)
+
+
 def test_force_large_cell_chunks():
     """A cell holding more particles than one shared-memory chunk (256) is processed in chunks."""
     rng = np.random.default_rng(8)
@@ -199,3 +207,19 @@ def test_full_size_ljc92k_counts_and_forces():
     sysm = systems.ljc92k()
     p = sysm.params(table_bins=512)
     F, Fo, o = _check_force(sysm, p)
+
+
+def test_full_size_ljc1m_pairs_and_reproducibility():
+    """1,048,576 atoms, 16 types, 22^3 cells: the pair total equals the oracle's (multi-threaded
+    half-shell count), and the fixed-point forces are bit-identical on a second evaluation."""
+    sysm = systems.ljc1m()
+    p = sysm.params(table_bins=512)
+    x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
+    with m.Context(p) as ctx:
+        F1, st, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        F2, _, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        o = oracle_from_ctx(ctx, sysm)
+    _, pairs = o.force_cells_mt(0)
+    assert st["pairs"] == pairs
+    assert np.array_equal(F1.view(np.uint32), F2.view(np.uint32))
+    assert np.isfinite(F1).all()
