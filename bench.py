@@ -318,6 +318,85 @@ def run_ours(args, rank, world, local, dist):
     return out
 
 
+def run_batch(args, rank, world, local, dist):
+    """512 independent replicas (N log-uniform 500-20,000, rc 10 A): all of them per step in one
+    graph launch, against the same replicas stepped one at a time (each its own graph)."""
+    import torch
+
+    import sc2019_md_gb300 as m
+    from sc2019_md_gb300 import systems
+
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    reps = systems.batch512(args.replicas)
+    gen_s = time.perf_counter() - t0
+    pos, vel, q, t, spec = systems.concat(reps)
+    params = reps[0].params(table_bins=args.bins, table_order=args.order, device=local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    b = m.Batch(params, spec)
+    lay = b.layout()
+    b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
+    b.step(args.warmup)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    dev_ms, pairs, pstep = 0.0, 0, []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = b.step(1)
+        dev_ms += st["device_ms"]
+        pairs += st["pairs_total"]
+        pstep.append(st["pairs"])
+    clk = clocks.stop()
+    fms = []
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        fms.append(b.time_force())
+    b.close()
+
+    # the same replicas one by one: a batch of one replica each, stepped in turn
+    k1 = max(3, min(args.steps, 20))
+    one_ms, one_pairs = 0.0, 0
+    for r, s in enumerate(reps):
+        with m.Batch(params, [spec[r]]) as b1:
+            b1.set_state(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.vel, s.q, s.type)
+            b1.step(1)
+            st = b1.step(k1)
+            one_ms += st["device_ms"]
+            one_pairs += st["pairs_total"]
+    value = pairs / (dev_ms * 1e-3)
+    ms_step = dev_ms / args.steps
+    force_s = float(np.mean(fms)) * 1e-3
+    props = torch.cuda.get_device_properties(local)
+    max_mhz = clk.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
+    achieved_tf = float(np.mean(pstep)) * FLOPS_PER_PAIR / force_s / 1e12
+    npath = np.bincount(lay["path"], minlength=3)
+    return {
+        "metric": "pair-evals/s, batched replicas (one launch per kernel per step) vs one by one",
+        "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded replicas)",
+        "config": {"workload": f"batch{len(reps)}: {len(reps)} replicas, {int(b.n)} atoms, N log-uniform "
+                               f"500-20000 at 0.1 /A^3, rc 10 A, argon-like +-0.42 e, order-{args.order} "
+                               f"{args.bins}-bin tables, int64 fixed point, velocity Verlet 2 fs",
+                   "paths": {"half_shell": int(npath[0]), "min_image": int(npath[1]), "all_images": int(npath[2])},
+                   "work_items": int(lay["total_items"]), "pairs_per_step": float(np.mean(pstep)),
+                   "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
+                   "generation_s": gen_s},
+        "one_by_one": {"value": one_pairs / (one_ms * 1e-3), "unit": "pair-evals/s", "steps": k1,
+                       "ms_per_step": one_ms / k1, "how": "a batch of one replica each, stepped in turn"},
+        "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tf / fp32_peak, "kernel": "k_force (batched work list)",
+                     "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR},
+        "gpu_launches": 9 * args.steps,
+        "clocks": clk,
+    }
+
+
 def oracle_system(sysm, order, bins, arith=0):
     import oracle
     T = len(sysm.sigma)
@@ -401,7 +480,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="ljc92k", choices=["ljc92k", "lj1728", "ljc1m"])
+    ap.add_argument("--workload", default="ljc92k", choices=["ljc92k", "lj1728", "ljc1m", "batch512"])
+    ap.add_argument("--replicas", type=int, default=512, help="batch512: number of replicas")
     ap.add_argument("--bins", type=int, default=512)
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -409,7 +489,12 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local, dist = dist_setup(args)
-    out = run_ours(args, rank, world, local, dist) if args.impl == "ours" else run_reference(args, rank, world)
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    elif args.workload == "batch512":
+        out = run_batch(args, rank, world, local, dist)
+    else:
+        out = run_ours(args, rank, world, local, dist)
     if rank == 0 and out is not None:
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -210,6 +210,49 @@ mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const float *x, 
                                    const float *z, const float *q, const int *type, float *fx,
                                    float *fy, float *fz, int64_t *pairs_out, void *stream);
 
+/* ---- batched independent replicas --------------------------------------------------------
+ * No counterpart in the reference (whose path is one system at a time).  A batch holds nrep
+ * periodic systems that share the force field of the params (types, cutoff, tables, arithmetic,
+ * integrator, dt, flags; box and ncell are per replica); every call covers all of them with one
+ * launch per kernel, and mdrl_batch_step replays a captured CUDA graph per step.
+ * Arrays are the replicas' particles concatenated in replica order (replica r owns
+ * [sum_{s<r} n_s, sum_{s<=r} n_s)), positions in [0, box_r).
+ * Replica paths: with at least 3 cells of edge >= rc per axis the half-shell traversal (forces,
+ * pair lists and trajectories equal to a single-system context's); with fewer (each box edge
+ * must still exceed rc) an all-pairs evaluation, by the one-wrap minimum image when every edge
+ * exceeds 2 rc, otherwise over every periodic image within rc.  MDRL_ACC_FIXED64 only. */
+typedef struct mdrl_batch mdrl_batch;
+
+typedef struct {
+    int n;            /* particles (>= 1) */
+    double box[3];    /* periodic box edges, each > cutoff */
+} mdrl_replica;
+
+enum { MDRL_PATH_HALF_SHELL = 0, MDRL_PATH_MIN_IMAGE = 1, MDRL_PATH_ALL_IMAGES = 2 };
+
+mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const mdrl_replica *reps,
+                              mdrl_batch **out);
+mdrl_status mdrl_batch_destroy(mdrl_batch *batch);
+/* Per replica (arrays of nrep, any may be NULL): the path, cells per axis [3*nrep], and work
+ * items of the force launch; *total_items the launch's grid. */
+mdrl_status mdrl_batch_layout(mdrl_batch *batch, int *path, int *ncell, int *items, int *total_items);
+/* One force evaluation of every replica on host arrays (see mdrl_force_eval). */
+mdrl_status mdrl_batch_force_eval(mdrl_batch *batch, const float *x, const float *y, const float *z,
+                                  const float *q, const int *type, float *fx, float *fy, float *fz,
+                                  int *counts, mdrl_stats *stats);
+/* Device-resident MD of every replica (see mdrl_set_state / mdrl_step / mdrl_get_state). */
+mdrl_status mdrl_batch_set_state(mdrl_batch *batch, const float *x, const float *y, const float *z,
+                                 const float *vx, const float *vy, const float *vz, const float *q,
+                                 const int *type);
+mdrl_status mdrl_batch_step(mdrl_batch *batch, int nsteps, mdrl_stats *stats);
+mdrl_status mdrl_batch_get_state(mdrl_batch *batch, float *x, float *y, float *z, float *vx,
+                                 float *vy, float *vz, float *fx, float *fy, float *fz);
+/* Per-replica totals (out[nrep]) of the last force evaluation: pairs, below_table, ncells and,
+ * with MDRL_FLAG_ENERGY, e_lj, e_coul, virial; kinetic from the current velocities. */
+mdrl_status mdrl_batch_replica_stats(mdrl_batch *batch, mdrl_stats *out);
+/* Device time of one force launch over the whole batch (see mdrl_time_force). */
+mdrl_status mdrl_batch_time_force(mdrl_batch *batch, float *ms);
+
 /* Drop-in for the reference C model's entry point.  Reads the argon PDB named by the
  * environment variable MDRL_INPUT (N from MDRL_N, default 500; iterations from MDRL_ITERS,
  * default 100), runs the reference's all-pairs direct FP32 force and symplectic-Euler update on

@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
         L.orc_force_cells_mt.restype = C.c_int64
         L.orc_force_allpairs_mt.argtypes = [C.POINTER(OrcSys), C.c_int, _F]
         L.orc_force_allpairs_mt.restype = C.c_int64
+        L.orc_force_allimage.argtypes = [C.POINTER(OrcSys), _D, _D, _D, _I, C.POINTER(OrcStats)]
+        L.orc_force_allimage.restype = C.c_int64
         L.orc_cmodel_run.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, _F, _F, _F, _I]
         _lib = L
     return _lib
@@ -124,6 +126,17 @@ class System:
         F = np.zeros((self.n, 3), np.float32)
         pairs = lib().orc_force_allpairs_mt(C.byref(self.s), nthreads, _p(F, _F))
         return F, pairs
+
+    def force_allimage(self):
+        """Every periodic image within rc (boxes with edge in (rc, 3 rc)): (F (n,3) FP64 table
+        evaluation, F32sum (n,3) FP64 sum of the ordered pairs' FP32 forces, Fabs (n,3),
+        counts (n,), stats)."""
+        F = np.zeros((self.n, 3)); F32 = np.zeros((self.n, 3)); A = np.zeros((self.n, 3))
+        cnt = np.zeros(self.n, np.int32); st = OrcStats()
+        r = lib().orc_force_allimage(C.byref(self.s), _p(F, _D), _p(F32, _D), _p(A, _D), _p(cnt, _I),
+                                     C.byref(st))
+        assert r >= 0
+        return F, F32, A, cnt, st.as_dict()
 
     def pair(self, xi, xj, qi=0.0, qj=0.0, ti=0, tj=0):
         out = np.zeros(8, np.float32)

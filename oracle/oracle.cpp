@@ -91,11 +91,18 @@ struct PairOut { float fx, fy, fz, fs, r2, elj, ec; int below; int dir[3]; float
  *   v_k = poly_k(r2) (tables) or the direct powers of 1/r2;
  *   fscal = ((QQ*v3) + B*v8) + A*v14, QQ = (ke*qi)*qj;  f = fscal * d.
  * In fused mode each "x*y + z" above is one fmaf. */
+inline int pair32_at(const orc_sys *s, float qi, int ti, float qj, int tj, PairOut *o);
+
 inline int pair32(const orc_sys *s, float xi, float yi, float zi, float qi, int ti, float xj,
                   float yj, float zj, float qj, int tj, PairOut *o) {
     o->dx = wrap1(xi - xj, s->box[0], &o->dir[0]);
     o->dy = wrap1(yi - yj, s->box[1], &o->dir[1]);
     o->dz = wrap1(zi - zj, s->box[2], &o->dir[2]);
+    return pair32_at(s, qi, ti, qj, tj, o);
+}
+
+/* The datapath from r2 on, for the difference already in o->dx, o->dy, o->dz. */
+inline int pair32_at(const orc_sys *s, float qi, int ti, float qj, int tj, PairOut *o) {
     const float r2 = add(add(mul(o->dx, o->dx), mul(o->dy, o->dy)), mul(o->dz, o->dz));
     o->r2 = r2;
     o->fx = o->fy = o->fz = o->fs = o->elj = o->ec = 0.0f;
@@ -431,6 +438,88 @@ int64_t orc_force_allpairs_mt(const orc_sys *s, int nthreads, float *F) {
         F[3 * i] = fx; F[3 * i + 1] = fy; F[3 * i + 2] = fz;
     }
     return pairs;
+}
+
+int64_t orc_force_allimage(const orc_sys *s, double *F, double *F32sum, double *Fabs, int *counts,
+                           orc_stats *st) {
+    if (!s || s->n < 0 || (s->n > 0 && (!s->x || !s->y || !s->z || !s->type))) return -1;
+    if (s->eval == 0 && (!s->tab || !s->pcoef64)) return -1;
+    const int n = s->n;
+    if (F) memset(F, 0, sizeof(double) * 3 * n);
+    if (F32sum) memset(F32sum, 0, sizeof(double) * 3 * n);
+    if (Fabs) memset(Fabs, 0, sizeof(double) * 3 * n);
+    if (counts) memset(counts, 0, sizeof(int) * n);
+    orc_stats acc;
+    memset(&acc, 0, sizeof(acc));
+    const float *p[3] = {s->x, s->y, s->z};
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            float cand[3][3];
+            int nc[3];
+            double shift[3][3];
+            for (int a = 0; a < 3; ++a) {
+                const float d0 = p[a][i] - p[a][j];
+                const float L = s->box[a];
+                const float c3[3] = {d0, d0 - L, d0 + L};
+                const double sh[3] = {0.0, -(double)L, (double)L};
+                nc[a] = 0;
+                for (int m = 0; m < 3; ++m)
+                    if (c3[m] * c3[m] <= s->rc2) { cand[a][nc[a]] = c3[m]; shift[a][nc[a]] = sh[m]; ++nc[a]; }
+            }
+            for (int ax = 0; ax < nc[0]; ++ax)
+                for (int ay = 0; ay < nc[1]; ++ay)
+                    for (int az = 0; az < nc[2]; ++az) {
+                        PairOut o;
+                        o.dx = cand[0][ax]; o.dy = cand[1][ay]; o.dz = cand[2][az];
+                        if (j > i) acc.candidates++;
+                        /* the FP32 datapath of the ordered pair (i's side: QQ = (ke*qi)*qj) */
+                        if (!pair32_at(s, qof(s, i), s->type[i], qof(s, j), s->type[j], &o)) continue;
+                        if (counts) counts[i]++;
+                        if (F32sum) { F32sum[3 * i] += o.fx; F32sum[3 * i + 1] += o.fy; F32sum[3 * i + 2] += o.fz; }
+                        if (Fabs) {
+                            Fabs[3 * i] += fabs(o.fx); Fabs[3 * i + 1] += fabs(o.fy); Fabs[3 * i + 2] += fabs(o.fz);
+                        }
+                        if (j < i) continue;
+                        acc.pairs++;
+                        acc.below_table += o.below;
+                        /* FP64 evaluation of the unordered pair at the exact difference */
+                        const double ex = (double)s->x[i] - (double)s->x[j] + shift[0][ax];
+                        const double ey = (double)s->y[i] - (double)s->y[j] + shift[1][ay];
+                        const double ez = (double)s->z[i] - (double)s->z[j] + shift[2][az];
+                        double e2 = ex * ex + ey * ey + ez * ez;
+                        const double *pc = s->pcoef64 + 4 * (s->type[i] * s->ntypes + s->type[j]);
+                        const double qq = s->ke64 * (double)qof(s, i) * (double)qof(s, j);
+                        double fs, el, ec = 0.0;
+                        if (s->eval == 0) {
+                            float r2e;
+                            int below;
+                            const int idx = table_index(s, o.r2, &r2e, &below);
+                            if (below) e2 = r2e;
+                            fs = pc[1] * poly64(s, ORC_F8, idx, e2) + pc[0] * poly64(s, ORC_F14, idx, e2);
+                            el = pc[3] * poly64(s, ORC_F6, idx, e2) + pc[2] * poly64(s, ORC_F12, idx, e2);
+                            if (s->ke != 0.0f) {
+                                fs += qq * poly64(s, ORC_F3, idx, e2);
+                                ec = qq * poly64(s, ORC_F1, idx, e2);
+                            }
+                        } else {
+                            const double i2 = 1.0 / e2, i4 = i2 * i2, i6 = i4 * i2, i8 = i4 * i4;
+                            const double i12 = i6 * i6, i14 = i12 * i2, i1 = sqrt(i2), i3 = i2 * i1;
+                            fs = (qq * i3 + pc[1] * i8) + pc[0] * i14;
+                            el = pc[3] * i6 + pc[2] * i12;
+                            ec = qq * i1;
+                        }
+                        acc.e_lj += el;
+                        acc.e_coul += ec;
+                        acc.virial += fs * e2;
+                        if (F) {
+                            F[3 * i] += fs * ex; F[3 * i + 1] += fs * ey; F[3 * i + 2] += fs * ez;
+                            F[3 * j] -= fs * ex; F[3 * j + 1] -= fs * ey; F[3 * j + 2] -= fs * ez;
+                        }
+                    }
+        }
+    if (st) *st = acc;
+    return acc.pairs;
 }
 
 /* SC/C_Model_ForceEval/MD_Evaluation_Model.cpp, restated.  Line numbers refer to that file.

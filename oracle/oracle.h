@@ -16,6 +16,10 @@
  *                      (home cell + 13 neighbours, Newton's third law to the neighbour)
  *   orc_force_direct64 FP64 direct LJ + Coulomb on the same pair set (the FP64 oracle)
  *   orc_force_tables64 FP64 evaluation of the same table polynomials (isolates FP32 error)
+ *   orc_force_allimage every periodic image within rc of every pair, for boxes whose edge lies in
+ *                      (rc, 3 rc) where the half shell does not apply (no counterpart in the
+ *                      reference, which requires 3 cells per axis; the pair datapath is
+ *                      orc_pair_f32's, the forces the FP64 table evaluation of orc_force_tables64)
  *   orc_cmodel_run     SC/C_Model_ForceEval/MD_Evaluation_Model.cpp:57-203, expression by expression
  *
  * Parity is pinned by the reference's own fixtures (tests/golden/, see make_golden.py) and by
@@ -88,6 +92,16 @@ int64_t orc_force_cells_mt(const orc_sys *s, int nthreads, int hbegin, int hend,
 /* All-pairs FP32 direct force (the C model's O(N^2) loop generalised to types and charges),
  * multi-threaded over i.  F[3n] float.  Returns the number of (ordered) pairs in cutoff. */
 int64_t orc_force_allpairs_mt(const orc_sys *s, int nthreads, float *F);
+
+/* All-image pairs: per axis the candidates fl(xi - xj), fl(. - L), fl(. + L) with
+ * fl(d*d) <= rc2; every combination with 0 < r2 <= rc2 (r2 = (dx*dx + dy*dy) + dz*dz in FP32,
+ * rounded per operation) is one pair.  Every ordered pair (i, j != i) runs the FP32 datapath from
+ * i's side (QQ = (ke*qi)*qj): F32sum[3i..] sums those FP32 forces in FP64 and Fabs their
+ * magnitudes, counts[i] the partners.  F is the FP64 table evaluation at the exact difference of
+ * each unordered pair (Newton's third law).  Any output may be NULL.  Returns the number of
+ * unordered pairs, -1 on error. */
+int64_t orc_force_allimage(const orc_sys *s, double *F, double *F32sum, double *Fabs, int *counts,
+                           orc_stats *st);
 
 /* The reference C model, restated: n particles (positions pos[3n], velocities vel[3n], both
  * updated in place), iters iterations, box edge and cutoff as given (the reference uses 24 and

@@ -15,7 +15,8 @@ import numpy as np
 
 __all__ = [
     "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables",
-    "cmodel_run", "md_evaluation_model", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
+    "cmodel_run", "md_evaluation_model", "Batch", "Replica", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
+    "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
     "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "MAX_TYPES", "STATUS",
 ]
@@ -75,6 +76,13 @@ _I = C.POINTER(C.c_int)
 _lib = None
 
 
+class Replica(C.Structure):
+    _fields_ = [("n", C.c_int), ("box", C.c_double * 3)]
+
+
+PATH_HALF_SHELL, PATH_MIN_IMAGE, PATH_ALL_IMAGES = 0, 1, 2
+
+
 def lib() -> C.CDLL:
     """The loaded libmdrl (raises when it has not been built)."""
     global _lib
@@ -109,6 +117,19 @@ def lib() -> C.CDLL:
     L.MD_Evaluation_Model.argtypes = []
     L.MD_Evaluation_Model.restype = C.c_int
     L.mdrl_cmodel_run.argtypes = [st, st, C.c_float, C.c_float, _F, _F, _F, _I]
+    L.mdrl_batch_create.argtypes = [C.POINTER(Params), st, C.POINTER(Replica), C.POINTER(vp)]
+    L.mdrl_batch_destroy.argtypes = [vp]
+    L.mdrl_batch_layout.argtypes = [vp, _I, _I, _I, _I]
+    L.mdrl_batch_force_eval.argtypes = [vp, _F, _F, _F, _F, _I, _F, _F, _F, _I, C.POINTER(Stats)]
+    L.mdrl_batch_set_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _I]
+    L.mdrl_batch_step.argtypes = [vp, st, C.POINTER(Stats)]
+    L.mdrl_batch_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
+    L.mdrl_batch_replica_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.mdrl_batch_time_force.argtypes = [vp, _F]
+    for name in ("mdrl_batch_create", "mdrl_batch_destroy", "mdrl_batch_layout", "mdrl_batch_force_eval",
+                 "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
+                 "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
+        getattr(L, name).restype = st
     for name in ("mdrl_fit_tables", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
                  "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
                  "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
@@ -291,6 +312,91 @@ class Context:
         a = [np.zeros(n, np.float32) for _ in range(9)]
         _check(lib().mdrl_get_state(self._h, *[_fp(v) for v in a]))
         return (np.stack(a[0:3], 1), np.stack(a[3:6], 1), np.stack(a[6:9], 1))
+
+
+class Batch:
+    """Independent periodic replicas sharing one force field (mdrl_batch_*).  `replicas` is a
+    sequence of (n, (Lx, Ly, Lz)); arrays are the replicas' particles concatenated in order."""
+
+    def __init__(self, params: Params, replicas):
+        self.params = params
+        reps = (Replica * len(replicas))()
+        for k, (n, box) in enumerate(replicas):
+            reps[k].n = int(n)
+            for d in range(3):
+                reps[k].box[d] = float(box[d])
+        self.nrep = len(replicas)
+        self.sizes = np.array([int(n) for n, _ in replicas], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+        self.n = int(self.offsets[-1])
+        self._h = C.c_void_p()
+        _check(lib().mdrl_batch_create(C.byref(params), self.nrep, reps, C.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().mdrl_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layout(self) -> dict:
+        path = np.zeros(self.nrep, np.int32)
+        ncell = np.zeros((self.nrep, 3), np.int32)
+        items = np.zeros(self.nrep, np.int32)
+        tot = C.c_int()
+        _check(lib().mdrl_batch_layout(self._h, _ip(path), _ip(ncell), _ip(items), C.byref(tot)))
+        return {"path": path, "ncell": ncell, "items": items, "total_items": tot.value}
+
+    def force(self, x, y, z, q=None, type=None, counts: bool = False):
+        n = self.n
+        x, y, z, q, t = _f32(x, n), _f32(y, n), _f32(z, n), _f32(q, n), _i32(type, n)
+        fx, fy, fz = (np.zeros(n, np.float32) for _ in range(3))
+        cnt = np.zeros(n, np.int32) if counts else None
+        st = Stats()
+        _check(lib().mdrl_batch_force_eval(self._h, _fp(x), _fp(y), _fp(z), _fp(q), _ip(t), _fp(fx), _fp(fy),
+                                           _fp(fz), _ip(cnt), C.byref(st)))
+        return np.stack([fx, fy, fz], axis=1), st.as_dict(), cnt
+
+    def set_state(self, x, y, z, v=None, q=None, type=None) -> None:
+        n = self.n
+        vx = vy = vz = None
+        if v is not None:
+            v = np.asarray(v, dtype=np.float32)
+            vx, vy, vz = (np.ascontiguousarray(v[:, k]) for k in range(3))
+        self._keep = (_f32(x, n), _f32(y, n), _f32(z, n), vx, vy, vz, _f32(q, n), _i32(type, n))
+        k = self._keep
+        _check(lib().mdrl_batch_set_state(self._h, _fp(k[0]), _fp(k[1]), _fp(k[2]), _fp(k[3]), _fp(k[4]),
+                                          _fp(k[5]), _fp(k[6]), _ip(k[7])))
+
+    def step(self, nsteps: int = 1) -> dict:
+        st = Stats()
+        _check(lib().mdrl_batch_step(self._h, nsteps, C.byref(st)))
+        return st.as_dict()
+
+    def state(self):
+        a = [np.zeros(self.n, np.float32) for _ in range(9)]
+        _check(lib().mdrl_batch_get_state(self._h, *[_fp(v) for v in a]))
+        return (np.stack(a[0:3], 1), np.stack(a[3:6], 1), np.stack(a[6:9], 1))
+
+    def replica_stats(self) -> list:
+        out = (Stats * self.nrep)()
+        _check(lib().mdrl_batch_replica_stats(self._h, out))
+        return [out[k].as_dict() for k in range(self.nrep)]
+
+    def time_force(self) -> float:
+        ms = C.c_float()
+        _check(lib().mdrl_batch_time_force(self._h, C.byref(ms)))
+        return ms.value
 
 
 def force_eval_static(params: Params, n: int, x, y, z, q, type, fx, fy, fz, stream=None) -> int:

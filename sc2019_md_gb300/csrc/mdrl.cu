@@ -15,8 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "mdrl_internal.h"
-#include "mdrl_force.cuh"
+#include "mdrl_ctx.cuh"
 
 using namespace mdrl;
 
@@ -24,93 +23,6 @@ namespace mdrl {
 static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 }  // namespace mdrl
-
-#define MDRL_CUDA(call)                                                                   \
-    do {                                                                                  \
-        cudaError_t e_ = (call);                                                          \
-        if (e_ != cudaSuccess) {                                                          \
-            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                \
-            return MDRL_ERR_CUDA;                                                         \
-        }                                                                                 \
-    } while (0)
-
-#define MDRL_TRY(expr)                         \
-    do {                                       \
-        mdrl_status s_ = (expr);               \
-        if (s_ != MDRL_OK) return s_;          \
-    } while (0)
-
-template <class T>
-static mdrl_status dalloc(T **p, size_t count) {
-    if (*p) { cudaFree(*p); *p = nullptr; }
-    if (count == 0) return MDRL_OK;
-    MDRL_CUDA(cudaMalloc((void **)p, sizeof(T) * count));
-    return MDRL_OK;
-}
-
-template <class T>
-static void dfree(T **p) {
-    if (*p) { cudaFree(*p); *p = nullptr; }
-}
-
-struct mdrl_ctx {
-    mdrl_params p;
-    Geom g;
-    int ncells = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaEvent_t evf0 = nullptr, evf1 = nullptr; /* around the force kernel */
-
-    /* tables */
-    int order = 1, nseg = 0, bins = 256, min_log2 = -2;
-    bool raw = false;
-    std::vector<float> tab;      /* canonical [6][order+1][nseg*bins] */
-    std::vector<float> pcoef;    /* [T*T*4] */
-    float ke = 0.0f;
-    float2 *d_f2 = nullptr, *d_e2 = nullptr;
-    float4 *d_f4 = nullptr, *d_e4 = nullptr;
-    float4 *d_fr = nullptr;      /* order 1: force functions packed per index (32 B) */
-    float4 *d_pcoef = nullptr;
-    MassTab mt_half, mt_full;
-
-    /* particle buffers */
-    int cap = 0, n = 0;
-    float *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_uq = nullptr;
-    int *d_ut = nullptr;
-    float *d_ox = nullptr, *d_oy = nullptr, *d_oz = nullptr; /* user-order outputs */
-    float *d_ovx = nullptr, *d_ovy = nullptr, *d_ovz = nullptr;
-    int *d_ocnt = nullptr;
-    float4 *d_pos[2] = {nullptr, nullptr}, *d_vel[2] = {nullptr, nullptr};
-    int *d_type[2] = {nullptr, nullptr}, *d_id[2] = {nullptr, nullptr};
-    int cur = 0;
-    int *d_cell_of = nullptr, *d_slot = nullptr, *d_tmp = nullptr, *d_sorted = nullptr;
-    int *d_count = nullptr, *d_start = nullptr;
-    unsigned *d_key = nullptr;   /* in-cell sort key (Morton code inside the cell) */
-    unsigned long long *d_F64 = nullptr;
-    float *d_F32 = nullptr;
-    unsigned long long *d_Fscr64 = nullptr; /* scratch accumulators for mdrl_time_force */
-    float *d_Fscr32 = nullptr;
-    int *d_cnt = nullptr;
-    UnitOut *d_unit = nullptr;
-    double *d_kepart = nullptr;
-    int kecap = 0;
-    DevTotals *d_tot = nullptr;
-    unsigned *d_err = nullptr;
-    int num_sms = 0;
-
-    /* pair-eval staging */
-    int pcap = 0;
-    float4 *d_pr = nullptr, *d_pn = nullptr, *d_pout = nullptr;
-    int *d_ptr = nullptr, *d_ptn = nullptr;
-    float2 *d_paux = nullptr;
-
-    /* state */
-    bool have_state = false;
-    cudaGraph_t graph[2] = {nullptr, nullptr};          /* one step from buffer slot k to 1-k */
-    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
-    int graph_n = -1;
-    bool graph_extra = false;
-};
 
 extern "C" const char *mdrl_version(void) { return "mdrl 0.1 (sm_103a)"; }
 
@@ -287,7 +199,7 @@ static mdrl_status upload_tables(mdrl_ctx *c) {
     return MDRL_OK;
 }
 
-static TableDev table_dev(const mdrl_ctx *c) {
+TableDev mdrl::table_dev(const mdrl_ctx *c) {
     TableDev t;
     t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4; t.fr = c->d_fr;
     t.order = c->order; t.nseg = c->nseg; t.bins = c->bins; t.lb = ilog2i(c->bins);
@@ -394,7 +306,7 @@ static mdrl_status ensure_cells(mdrl_ctx *c) {
     return MDRL_OK;
 }
 
-static mdrl_status ensure_capacity(mdrl_ctx *c, int n) {
+mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
     MDRL_TRY(ensure_cells(c));
     if (n <= c->cap) return MDRL_OK;
     free_particles(c);
@@ -435,7 +347,21 @@ force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap) {
 }
 }  // namespace mdrl
 
-static int eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
+/* The smem attribute is set once per kernel and device, on the first (uncaptured) launch. */
+mdrl_status mdrl::prepare_force_kernel(force_fn fn, int device) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    const std::pair<const void *, int> key((const void *)fn, device);
+    if (!done.count(key)) {
+        MDRL_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)force_smem_bytes(MDRL_MAX_TYPES, true)));
+        done.insert(key);
+    }
+    return MDRL_OK;
+}
+
+int mdrl::eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
 
 static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra,
                                      unsigned long long *F64, float *F32) {
@@ -443,22 +369,11 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
     const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
     force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra);
-    /* The smem attribute is set once per kernel and device, on the first (uncaptured) launch. */
-    {
-        static std::mutex mu;
-        static std::set<std::pair<const void *, int>> done;
-        std::lock_guard<std::mutex> lock(mu);
-        const std::pair<const void *, int> key((const void *)fn, c->p.device);
-        if (!done.count(key)) {
-            MDRL_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)force_smem_bytes(MDRL_MAX_TYPES, true)));
-            done.insert(key);
-        }
-    }
+    MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<units, kFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
-                                         c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit);
+                                         c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -468,7 +383,6 @@ static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int
     return launch_force_into(c, n, pos, type, extra, c->d_F64, c->d_F32);
 }
 
-static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 
 
@@ -496,7 +410,7 @@ static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, 
     return MDRL_OK;
 }
 
-static mdrl_status check_device_errors(mdrl_ctx *c) {
+mdrl_status mdrl::check_device_errors(mdrl_ctx *c) {
     unsigned err = 0;
     MDRL_CUDA(cudaMemcpy(&err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (err & kErrPosition) {

@@ -45,13 +45,18 @@ constexpr int kFW = MDRL_FORCE_WARPS;  /* warps per force CTA */
 constexpr int kFT = kFW * 32;
 constexpr int kStepsPerPiece = 6;      /* j-steps (of 8 particles) per piece */
 
+struct BatchRep;
+struct BatchItem;
 typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
-                         int, float, int, unsigned long long *, float *, int *, UnitOut *);
+                         int, float, int, unsigned long long *, float *, int *, UnitOut *,
+                         const BatchItem *, const BatchRep *);
 
 /* Work items (one per unit): the result slots k_totals sums. */
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
 
 force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap);
+/* the batched-replica instantiation (int64 fixed point, per-pair wrap) */
+force_fn pick_force_batch(int order, bool sep, bool extra);
 
 inline size_t force_smem_bytes(int ntypes, bool extra) {
     return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
@@ -173,41 +178,131 @@ __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32,
     }
 }
 
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP>
-__global__ void __launch_bounds__(kFT, 16 / kFW)
-k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
-        const int *__restrict__ cstart, Geom g, TableDev tab, const float4 *__restrict__ pcoef,
-        int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
-        float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout) {
-    extern __shared__ float4 smem[];
-    float4 *sIp = smem;
-    float4 *sJp = sIp + kChunk;
-    float4 *sCoef = sJp + kChunk;
-    int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
-    int *sJt = sIt + kChunk;
-    float *sF = reinterpret_cast<float *>(sJt + kChunk);             /* [kFW][2][3][kChunk] */
-    int *sC = reinterpret_cast<int *>(sF + kFW * 6 * kChunk);       /* [kFW][2][kChunk] */
-    __shared__ double s_red[kFW][3];
-    __shared__ unsigned long long s_cnt[kFW][2];
+/* ---- batched replicas ----------------------------------------------------------------------
+ * One launch covers every replica of a batch; a work item is one of
+ *   (replica, half-shell unit)  at least 3 cells of edge >= rc per axis: the path below with the
+ *                               replica's geometry and cell offset (per-pair wrap);
+ *   (replica, cell pair a <= b) every edge above 2 rc but fewer cells: the same tiled Newton-3
+ *                               path over an explicit pair of cells, per-pair minimum image;
+ *   (replica, kFT particles)    an edge of at most 2 rc (always above rc): every periodic image
+ *                               within rc, all_images_body. */
+enum : int { kPathHalfShell = 0, kPathMinImage = 1, kPathAllImages = 2 };
 
+struct BatchRep {
+    Geom g;
+    int cell_off;    /* first global cell of the replica */
+    int p_off, n;    /* its particles: [p_off, p_off + n) of the cell-sorted arrays */
+    int path;        /* kPath* */
+};
+
+struct BatchItem {
+    int rep;
+    int unit;        /* half-shell unit, or first particle (relative) of an all-pairs block */
+};
+
+/* Forces of a replica with a box edge of at most 2 rc (always above rc), where more than one
+ * periodic image of a pair can lie within rc.  Per axis the candidates are fl(xi - xj),
+ * fl(. - L), fl(. + L) with fl(d*d) <= rc2 (a necessary condition for r2 <= rc2, since r2 >=
+ * each rounded square); every combination with 0 < r2 <= rc2 is a pair, and at most two
+ * candidates pass per axis because the edge exceeds rc.  Thread t owns particle i = b0 + t and
+ * sums f_ij over every j != i and image, each ordered pair evaluated from i's side
+ * (QQ = (ke*qi)*qj), so the particle's force is complete and is stored without atomics;
+ * energies and the virial carry a factor 1/2, and pairs count j > i. */
+template <int ORDER, bool SEP, bool EXTRA>
+__device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, const int *__restrict__ ptype,
+                                                   const BatchRep &rp, int b0, TableDev tab,
+                                                   const float4 *sCoef, int ntypes, float ke, int ntot,
+                                                   unsigned long long *__restrict__ F64,
+                                                   int *__restrict__ counts, float4 *sJp, int *sJt,
+                                                   float &acc_elj, float &acc_ec, float &acc_vir,
+                                                   unsigned &acc_pairs, unsigned &acc_below) {
+    const Geom &g = rp.g;
+    const int tid = threadIdx.x;
+    const int i = b0 + tid;
+    const bool have = i < rp.n;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    int ti = 0;
+    if (have) { pi = pos[rp.p_off + i]; ti = ptype[rp.p_off + i] * ntypes; }
+    const float qi = __fmul_rn(ke, pi.w);
+    const bool coul = ke != 0.0f;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    int cnt = 0;
+    auto eval = [&](float dx, float dy, float dz, float r2, float qj, int tj, bool upper) {
+        float v14, v8, v3, v12, v6, v1;
+        pair_functions_fast<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1);
+        const float4 pc = sCoef[ti + tj];
+        const float qq = __fmul_rn(qi, qj);
+        const float fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
+        fx += __fmul_rn(fs, dx); fy += __fmul_rn(fs, dy); fz += __fmul_rn(fs, dz);
+        if (upper) ++acc_pairs;
+        if (EXTRA) {
+            ++cnt;
+            if (upper) acc_below += (ORDER > 0 && r2 < tab.r2min) ? 1u : 0u;
+            acc_elj += 0.5f * combine_elj<SEP>(pc, v12, v6);
+            if (coul) acc_ec += 0.5f * __fmul_rn(qq, v1);
+            acc_vir += 0.5f * __fmul_rn(fs, r2);
+        }
+    };
+    for (int j0 = 0; j0 < rp.n; j0 += kFT) {
+        const int nj = min(kFT, rp.n - j0);
+        __syncthreads();
+        if (tid < nj) { sJp[tid] = pos[rp.p_off + j0 + tid]; sJt[tid] = ptype[rp.p_off + j0 + tid]; }
+        __syncthreads();
+        if (!have) continue;
+        for (int jj = 0; jj < nj; ++jj) {
+            const int j = j0 + jj;
+            if (j == i) continue;
+            const float4 pj = sJp[jj];
+            float c[3][2];
+            int nc[3];
+            const float d0[3] = {__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z)};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float cand[3] = {d0[a], __fsub_rn(d0[a], g.L[a]), __fadd_rn(d0[a], g.L[a])};
+                int k = 0;
+                c[a][0] = c[a][1] = 0.0f;
+#pragma unroll
+                for (int m = 0; m < 3; ++m)
+                    if (__fmul_rn(cand[m], cand[m]) <= g.rc2 && k < 2) {
+                        if (k == 0) c[a][0] = cand[m]; else c[a][1] = cand[m];
+                        ++k;
+                    }
+                nc[a] = k;
+            }
+            for (int ax = 0; ax < nc[0]; ++ax)
+                for (int ay = 0; ay < nc[1]; ++ay)
+                    for (int az = 0; az < nc[2]; ++az) {
+                        const float dx = ax ? c[0][1] : c[0][0];
+                        const float dy = ay ? c[1][1] : c[1][0];
+                        const float dz = az ? c[2][1] : c[2][0];
+                        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        if (r2 > 0.0f && r2 <= g.rc2) eval(dx, dy, dz, r2, pj.w, sJt[jj], j > i);
+                    }
+        }
+    }
+    if (have) {
+        const size_t gi = (size_t)rp.p_off + i;
+        F64[gi] = to_fixed(fx);
+        F64[(size_t)ntot + gi] = to_fixed(fy);
+        F64[2 * (size_t)ntot + gi] = to_fixed(fz);
+        if (EXTRA) counts[gi] = cnt;
+    }
+}
+
+/* One unit: home-cell particles [hs, hs + ni_all) against neighbour-cell particles
+ * [cs, cs + nj_all) (the same cell when self), per-unit shift (sx, sy, sz) or, with WRAP, the
+ * per-pair one-wrap rule; writes the unit's totals to uout[blockIdx.x]. */
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP>
+__device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const int *__restrict__ ptype,
+                                           int hs, int ni_all, int cs, int nj_all, bool self, const Geom &g,
+                                           float sx, float sy, float sz, const TableDev &tab,
+                                           const float4 *__restrict__ pcoef, int ntypes, float ke, int n,
+                                           unsigned long long *__restrict__ F64, float *__restrict__ F32,
+                                           int *__restrict__ counts, UnitOut *__restrict__ uout, float4 *sIp,
+                                           float4 *sJp, float4 *sCoef, int *sIt, int *sJt, float *sF, int *sC,
+                                           double (*s_red)[3], unsigned long long (*s_cnt)[2]) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
-    const int unit = blockIdx.x;
-    const int h = unit / kHalfShellCells, f = unit - h * kHalfShellCells;
-    const int nyz = g.nc[1] * g.nc[2];
-    const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
-    int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
-    /* neighbour across the +L face: its particles sit at x + L, so d = xi - xj - L */
-    const float sx = cx >= g.nc[0] ? -g.L[0] : (cx < 0 ? g.L[0] : 0.0f);
-    const float sy = cy >= g.nc[1] ? -g.L[1] : (cy < 0 ? g.L[1] : 0.0f);
-    const float sz = cz >= g.nc[2] ? -g.L[2] : (cz < 0 ? g.L[2] : 0.0f);
-    cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
-    cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
-    cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
-    const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
-    const bool self = (f == 0);
-    const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
-    const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
     const bool coul = ke != 0.0f;
     const float far = 1.0e18f;   /* padding lanes: finite, so r2 ~ 3e36 > rc2 */
     float *wFi = sF + warp * 6 * kChunk;
@@ -420,7 +515,119 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
             u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
             u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
         }
-        uout[unit] = u;
+        uout[blockIdx.x] = u;
+    }
+}
+
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false>
+__global__ void __launch_bounds__(kFT, 16 / kFW)
+k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
+        const int *__restrict__ cstart, Geom gparam, TableDev tab, const float4 *__restrict__ pcoef,
+        int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
+        float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout,
+        const BatchItem *__restrict__ items = nullptr, const BatchRep *__restrict__ reps = nullptr) {
+    extern __shared__ float4 smem[];
+    float4 *sIp = smem;
+    float4 *sJp = sIp + kChunk;
+    float4 *sCoef = sJp + kChunk;
+    int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
+    int *sJt = sIt + kChunk;
+    float *sF = reinterpret_cast<float *>(sJt + kChunk);             /* [kFW][2][3][kChunk] */
+    int *sC = reinterpret_cast<int *>(sF + kFW * 6 * kChunk);       /* [kFW][2][kChunk] */
+    __shared__ double s_red[kFW][3];
+    __shared__ unsigned long long s_cnt[kFW][2];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int row = lane >> 3, col = lane & 7;
+    int unit = blockIdx.x, coff = 0;
+    bool cell_pair = false, use_wrap = WRAP;
+    Geom gb;
+    if (BATCH) {
+        const BatchItem it = items[blockIdx.x];
+        const BatchRep rp = reps[it.rep];
+        if (rp.path == kPathAllImages) {
+            for (int t = tid; t < ntypes * ntypes; t += kFT) sCoef[t] = pcoef[t];
+            float e1 = 0.f, e2 = 0.f, e3 = 0.f;
+            unsigned c1 = 0, c2 = 0;
+            all_images_body<ORDER, SEP, EXTRA>(pos, ptype, rp, it.unit, tab, sCoef, ntypes, ke, n, F64, counts,
+                                                  sJp, sJt, e1, e2, e3, c1, c2);
+            double d1 = e1, d2 = e2, d3 = e3;
+            unsigned long long u1 = c1, u2 = c2;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                u1 += __shfl_xor_sync(0xffffffffu, u1, o);
+                if (EXTRA) {
+                    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+                    d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+                    d3 += __shfl_xor_sync(0xffffffffu, d3, o);
+                    u2 += __shfl_xor_sync(0xffffffffu, u2, o);
+                }
+            }
+            if (lane == 0) {
+                s_red[warp][0] = d1; s_red[warp][1] = d2; s_red[warp][2] = d3;
+                s_cnt[warp][0] = u1; s_cnt[warp][1] = u2;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                UnitOut u;
+                u.e_lj = u.e_coul = u.virial = 0.0;
+                u.pairs = u.below = 0ull;
+                for (int w = 0; w < kFW; ++w) {
+                    u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
+                    u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
+                }
+                uout[blockIdx.x] = u;
+            }
+            return;
+        }
+        gb = rp.g;
+        unit = it.unit;
+        coff = rp.cell_off;
+        cell_pair = rp.path == kPathMinImage;
+        /* the per-unit shift needs >= 4 cells per axis; 3-cell grids and cell pairs wrap per pair */
+        use_wrap = cell_pair || gb.nc[0] < 4 || gb.nc[1] < 4 || gb.nc[2] < 4;
+    }
+    const Geom &g = BATCH ? gb : gparam;
+    int h, c;
+    bool self;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    if (BATCH && cell_pair) {
+        /* an explicit pair of the replica's cells, every pair with the per-pair minimum image */
+        const int nct = g.nc[0] * g.nc[1] * g.nc[2];
+        h = unit / nct;
+        c = unit - h * nct;
+        self = h == c;
+    } else {
+        h = unit / kHalfShellCells;
+        const int f = unit - h * kHalfShellCells;
+        const int nyz = g.nc[1] * g.nc[2];
+        const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
+        int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
+        /* neighbour across the +L face: its particles sit at x + L, so d = xi - xj - L */
+        sx = cx >= g.nc[0] ? -g.L[0] : (cx < 0 ? g.L[0] : 0.0f);
+        sy = cy >= g.nc[1] ? -g.L[1] : (cy < 0 ? g.L[1] : 0.0f);
+        sz = cz >= g.nc[2] ? -g.L[2] : (cz < 0 ? g.L[2] : 0.0f);
+        cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
+        cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
+        cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
+        c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
+        self = (f == 0);
+    }
+    const int hs = cstart[coff + h], ni_all = cstart[coff + h + 1] - hs;
+    const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
+    if constexpr (BATCH) {
+        if (use_wrap)
+            force_unit<ORDER, SEP, EXTRA, ACC, true>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+                                                     pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
+                                                     sCoef, sIt, sJt, sF, sC, s_red, s_cnt);
+        else
+            force_unit<ORDER, SEP, EXTRA, ACC, false>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+                                                      pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
+                                                      sCoef, sIt, sJt, sF, sC, s_red, s_cnt);
+    } else {
+        force_unit<ORDER, SEP, EXTRA, ACC, WRAP>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+                                                 pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp, sCoef,
+                                                 sIt, sJt, sF, sC, s_red, s_cnt);
     }
 }
 

@@ -27,4 +27,21 @@ force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap) {
     }
 }
 
+template <int ORDER>
+static force_fn pick_batch_order(bool sep, bool extra) {
+    if (sep) return extra ? (force_fn)k_force<ORDER, true, true, 0, true, true>
+                          : (force_fn)k_force<ORDER, true, false, 0, true, true>;
+    return extra ? (force_fn)k_force<ORDER, false, true, 0, true, true>
+                 : (force_fn)k_force<ORDER, false, false, 0, true, true>;
+}
+
+force_fn pick_force_batch(int order, bool sep, bool extra) {
+    switch (order) {
+        case 0: return pick_batch_order<0>(sep, extra);
+        case 1: return pick_batch_order<1>(sep, extra);
+        case 2: return pick_batch_order<2>(sep, extra);
+        default: return pick_batch_order<3>(sep, extra);
+    }
+}
+
 }  // namespace mdrl

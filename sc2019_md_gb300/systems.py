@@ -13,6 +13,12 @@ Workloads (all periodic):
   ljc1m       1,048,576 atoms in a 224 A cube, rc 10 (22^3 cells), 16 types, charges U(-0.8, 0.8)
               shifted to net zero; 1.0 A minimum separation as for ljc92k (without one, random
               overlaps give pair forces beyond the int64 fixed-point range).
+  batch512    512 independent replicas, N log-uniform in [500, 20000] (sizes drawn from seed
+              20191117 + 4), cubic box L = (N / 0.1)^(1/3), rc 10; each replica (seed
+              20191117 + 4 + 1000 r) is argon-like (sigma 3.4, epsilon 0.238, 39.95 amu) with
+              +-0.42 e net-neutral charges, placed uniformly with a 1.0 A minimum separation.
+              Replicas below ~2,700 atoms have fewer than 3 cells per axis, and below ~800 the
+              box edge is under 2 rc.
 """
 from __future__ import annotations
 
@@ -152,3 +158,40 @@ def small_ljc(n: int, L: float, cutoff: float, seed: int, ntypes: int = 4,
     nc = int(np.floor(np.float32(L) / np.float32(cutoff)))
     return System("small_ljc", box, cutoff, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
                   q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+
+
+def replica(n: int, r: int, density: float = 0.1, cutoff: float = 10.0, dmin: float = 1.0) -> System:
+    """Replica r of the batched workload: n argon-like atoms with +-0.42 e charges in a cube
+    at `density`."""
+    rng = np.random.default_rng(20191117 + 4 + 1000 * r)
+    L = float((n / density) ** (1.0 / 3.0))
+    box = (L, L, L)
+    pos = wrap_into_box(uniform_min_sep(n, box, dmin, rng), box)
+    q = np.full(n, 0.42)
+    q[: n // 2] = -0.42
+    if n % 2:
+        q[-1] = 0.0
+    rng.shuffle(q)
+    m = np.full(n, 39.95)
+    nc = max(1, int(np.floor(np.float32(L) / np.float32(cutoff))))
+    return System(f"replica{r}", box, cutoff, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
+                  q.astype(np.float32), np.zeros(n, np.int32), [3.4], [0.238], [39.95], COULOMB_K)
+
+
+def batch_sizes(count: int = 512, lo: int = 500, hi: int = 20000) -> np.ndarray:
+    """Replica sizes of the batched workload: log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(20191117 + 4)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), count)).round().astype(np.int64)
+
+
+def batch512(count: int = 512) -> list:
+    return [replica(int(n), r) for r, n in enumerate(batch_sizes(count))]
+
+
+def concat(reps: list):
+    """Concatenated arrays of a replica list: (pos, vel, q, type, [(n, box), ...])."""
+    pos = np.concatenate([s.pos for s in reps]).astype(np.float32)
+    vel = np.concatenate([s.vel for s in reps]).astype(np.float32)
+    q = np.concatenate([s.q for s in reps]).astype(np.float32)
+    t = np.concatenate([s.type for s in reps]).astype(np.int32)
+    return pos, vel, q, t, [(s.n, s.box) for s in reps]

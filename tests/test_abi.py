@@ -35,9 +35,10 @@ def test_python_mirror_binds_every_symbol():
 
 
 def test_struct_layouts_match_header():
-    """Field order and count of mdrl_params / mdrl_stats in the header equal the mirror's."""
+    """Field order and count of mdrl_params / mdrl_stats / mdrl_replica in the header equal the
+    mirror's."""
     text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "mdrl.h").read_text(), flags=re.S)
-    for cname, cls in (("mdrl_params", m.Params), ("mdrl_stats", m.Stats)):
+    for cname, cls in (("mdrl_params", m.Params), ("mdrl_stats", m.Stats), ("mdrl_replica", m.Replica)):
         body = re.search(r"typedef struct \{((?:(?!typedef struct).)*?)\}\s*" + cname + ";", text, re.S).group(1)
         fields = []
         for decl in body.split(";"):
@@ -76,3 +77,28 @@ def test_null_context_calls_fail_cleanly():
     h = C.c_void_p()
     assert L.mdrl_create(C.byref(p), C.byref(h)) == 1
     assert b"box" in L.mdrl_last_error()
+
+
+def test_batch_validation_before_any_device_call():
+    """mdrl_batch_create rejects bad replicas and modes on the host, before touching a GPU."""
+    L = m.lib()
+    h = C.c_void_p()
+    p = m.default_params(cutoff=10.0)
+    reps = (m.Replica * 2)()
+    reps[0].n, reps[1].n = 100, 100
+    for d in range(3):
+        reps[0].box[d] = 20.0
+        reps[1].box[d] = 9.5          # not above the cutoff
+    assert L.mdrl_batch_create(C.byref(p), 2, reps, C.byref(h)) == 3
+    assert b"replica 1" in L.mdrl_last_error() and b"exceed the cutoff" in L.mdrl_last_error()
+    for d in range(3):
+        reps[1].box[d] = 20.0
+    reps[1].n = 0
+    assert L.mdrl_batch_create(C.byref(p), 2, reps, C.byref(h)) == 1
+    reps[1].n = 100
+    p.accum = m.ACC_FP32_ATOMIC
+    assert L.mdrl_batch_create(C.byref(p), 2, reps, C.byref(h)) == 1
+    assert b"fixed point" in L.mdrl_last_error()
+    assert L.mdrl_batch_create(C.byref(p), 0, reps, C.byref(h)) == 1
+    assert L.mdrl_batch_destroy(None) == 0
+    assert L.mdrl_batch_step(None, 1, None) == 1
