@@ -201,9 +201,10 @@ def run_ours(args, rank, world, local, dist):
         if dist is not None:
             dist.barrier()
 
-    # ---- tuned: int64 fixed point ----------------------------------------------------------
+    # ---- tuned: int64 fixed point, autotuned tile -------------------------------------------
     ctx = m.Context(params)
     ctx.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
+    tune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile(), "ms": None, "default_ms": None}
     timed_steps(ctx, args.warmup)
     barrier()
     clocks = Clocks(local)
@@ -291,10 +292,14 @@ def run_ours(args, rank, world, local, dist):
         "data": "synthetic (seeded; shapes of the reference's ApoA1 dataset)",
         "config": {"workload": workload_desc(sysm, params.table_order, params.table_bins),
                    "accumulation": "int64 fixed point 2^-24 (tuned)", "parallelism": f"replicas x{world}",
+                   "tile": {"warps_per_cta": tune["tile"][0], "steps_per_piece": tune["tile"][1],
+                            "autotuned": not args.no_tune, "force_ms_tuned": tune["ms"],
+                            "force_ms_default_tile": tune["default_ms"]},
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
                    "pairs_per_step": pairs_launch},
         "plain": {"value": float(psum[2]) / (float(emax[1]) * 1e-3), "unit": "pair-evals/s",
-                  "ms_per_step": float(emax[1]) / kp, "accumulation": "FP32 atomics", "steps": kp,
+                  "ms_per_step": float(emax[1]) / kp, "accumulation": "FP32 atomics, default tile (4 warps, 6 steps)",
+                  "steps": kp,
                   "force_ms": float(np.mean(pfms))},
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak, "traffic": committed_traffic(args.workload),
@@ -337,6 +342,7 @@ def run_batch(args, rank, world, local, dist):
     b = m.Batch(params, spec)
     lay = b.layout()
     b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
+    tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6), "ms": None, "default_ms": None}
     b.step(args.warmup)
     torch.cuda.synchronize()
     clocks = Clocks(local)
@@ -385,10 +391,13 @@ def run_batch(args, rank, world, local, dist):
                                f"{args.bins}-bin tables, int64 fixed point, velocity Verlet 2 fs",
                    "paths": {"half_shell": int(npath[0]), "min_image": int(npath[1]), "all_images": int(npath[2])},
                    "work_items": int(lay["total_items"]), "pairs_per_step": float(np.mean(pstep)),
+                   "tile": {"steps_per_piece": tune["tile"][1], "autotuned": not args.no_tune,
+                            "force_ms_tuned": tune["ms"], "force_ms_default_tile": tune["default_ms"]},
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
                    "generation_s": gen_s},
         "one_by_one": {"value": one_pairs / (one_ms * 1e-3), "unit": "pair-evals/s", "steps": k1,
-                       "ms_per_step": one_ms / k1, "how": "a batch of one replica each, stepped in turn"},
+                       "ms_per_step": one_ms / k1,
+                       "how": "a batch of one replica each (default tile), stepped in turn, each its own graph"},
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak, "kernel": "k_force (batched work list)",
                      "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR},
@@ -485,6 +494,7 @@ def main():
     ap.add_argument("--bins", type=int, default=512)
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tile (no autotuning)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -115,6 +115,13 @@ typedef struct {
 
 typedef struct mdrl_ctx mdrl_ctx;
 
+/* Tile of the half-shell force kernel: warps per CTA (4, or 8 with MDRL_ACC_FIXED64 outside a
+ * batch) and j-steps of 8 particles per work piece (1..32).  Default {4, 6}. */
+typedef struct {
+    int warps_per_cta;
+    int steps_per_piece;
+} mdrl_tile;
+
 /* Library identity and the last error text of the calling thread ("" when none). */
 const char *mdrl_version(void);
 const char *mdrl_last_error(void);
@@ -252,6 +259,25 @@ mdrl_status mdrl_batch_get_state(mdrl_batch *batch, float *x, float *y, float *z
 mdrl_status mdrl_batch_replica_stats(mdrl_batch *batch, mdrl_stats *out);
 /* Device time of one force launch over the whole batch (see mdrl_time_force). */
 mdrl_status mdrl_batch_time_force(mdrl_batch *batch, float *ms);
+
+/* ---- tiles and the autotuner ---------------------------------------------------------------
+ * No counterpart in the reference.  mdrl_autotune times the force kernel (mdrl_time_force's
+ * launch, median of 5) for every candidate tile on the context's current state (call it after
+ * mdrl_set_state), keeps the fastest and returns it with its time and the default tile's time.
+ * Candidates: warps per CTA {4, 8} (8 with MDRL_ACC_FIXED64 only) x steps per piece
+ * {3, 4, 6, 8, 12}.  Results are cached per process under a key of the cell grid, mean cell
+ * occupancy (to 1/8), types, table order and bins, arithmetic, accumulation and Coulomb on/off;
+ * a cached key is reused without timing unless flags has MDRL_TUNE_RETIME.  When the environment
+ * variable MDRL_TUNE_CACHE names a file, results are appended to it and read back by later
+ * processes.  The tile is part of the captured step graph, which is re-captured after a change. */
+#define MDRL_TUNE_RETIME 1
+mdrl_status mdrl_set_tile(mdrl_ctx *ctx, const mdrl_tile *tile);
+mdrl_status mdrl_get_tile(mdrl_ctx *ctx, mdrl_tile *tile);
+mdrl_status mdrl_autotune(mdrl_ctx *ctx, int flags, mdrl_tile *best, float *best_ms, float *default_ms);
+/* The same for a batch (4 warps per CTA; steps per piece tuned), after mdrl_batch_set_state. */
+mdrl_status mdrl_batch_set_tile(mdrl_batch *batch, const mdrl_tile *tile);
+mdrl_status mdrl_batch_autotune(mdrl_batch *batch, int flags, mdrl_tile *best, float *best_ms,
+                                float *default_ms);
 
 /* Drop-in for the reference C model's entry point.  Reads the argon PDB named by the
  * environment variable MDRL_INPUT (N from MDRL_N, default 500; iterations from MDRL_ITERS,

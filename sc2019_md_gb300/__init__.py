@@ -15,7 +15,7 @@ import numpy as np
 
 __all__ = [
     "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables",
-    "cmodel_run", "md_evaluation_model", "Batch", "Replica", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
+    "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
     "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
     "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "MAX_TYPES", "STATUS",
@@ -76,6 +76,16 @@ _I = C.POINTER(C.c_int)
 _lib = None
 
 
+class Tile(C.Structure):
+    _fields_ = [("warps_per_cta", C.c_int), ("steps_per_piece", C.c_int)]
+
+    def as_tuple(self):
+        return (self.warps_per_cta, self.steps_per_piece)
+
+
+TUNE_RETIME = 1
+
+
 class Replica(C.Structure):
     _fields_ = [("n", C.c_int), ("box", C.c_double * 3)]
 
@@ -126,7 +136,13 @@ def lib() -> C.CDLL:
     L.mdrl_batch_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
     L.mdrl_batch_replica_stats.argtypes = [vp, C.POINTER(Stats)]
     L.mdrl_batch_time_force.argtypes = [vp, _F]
-    for name in ("mdrl_batch_create", "mdrl_batch_destroy", "mdrl_batch_layout", "mdrl_batch_force_eval",
+    L.mdrl_set_tile.argtypes = [vp, C.POINTER(Tile)]
+    L.mdrl_get_tile.argtypes = [vp, C.POINTER(Tile)]
+    L.mdrl_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
+    L.mdrl_batch_set_tile.argtypes = [vp, C.POINTER(Tile)]
+    L.mdrl_batch_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
+    for name in ("mdrl_set_tile", "mdrl_get_tile", "mdrl_autotune", "mdrl_batch_set_tile", "mdrl_batch_autotune",
+                 "mdrl_batch_create", "mdrl_batch_destroy", "mdrl_batch_layout", "mdrl_batch_force_eval",
                  "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
                  "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
         getattr(L, name).restype = st
@@ -307,6 +323,21 @@ class Context:
         _check(lib().mdrl_time_force(self._h, C.byref(ms)))
         return ms.value
 
+    def set_tile(self, warps_per_cta: int, steps_per_piece: int) -> None:
+        t = Tile(warps_per_cta, steps_per_piece)
+        _check(lib().mdrl_set_tile(self._h, C.byref(t)))
+
+    def tile(self) -> tuple:
+        t = Tile()
+        _check(lib().mdrl_get_tile(self._h, C.byref(t)))
+        return t.as_tuple()
+
+    def autotune(self, retime: bool = False) -> dict:
+        """Time every candidate tile on the current state and keep the fastest."""
+        t, b, d = Tile(), C.c_float(), C.c_float()
+        _check(lib().mdrl_autotune(self._h, TUNE_RETIME if retime else 0, C.byref(t), C.byref(b), C.byref(d)))
+        return {"tile": t.as_tuple(), "ms": b.value, "default_ms": d.value}
+
     def state(self):
         n = self._n
         a = [np.zeros(n, np.float32) for _ in range(9)]
@@ -397,6 +428,15 @@ class Batch:
         ms = C.c_float()
         _check(lib().mdrl_batch_time_force(self._h, C.byref(ms)))
         return ms.value
+
+    def set_tile(self, warps_per_cta: int, steps_per_piece: int) -> None:
+        t = Tile(warps_per_cta, steps_per_piece)
+        _check(lib().mdrl_batch_set_tile(self._h, C.byref(t)))
+
+    def autotune(self, retime: bool = False) -> dict:
+        t, b, d = Tile(), C.c_float(), C.c_float()
+        _check(lib().mdrl_batch_autotune(self._h, TUNE_RETIME if retime else 0, C.byref(t), C.byref(b), C.byref(d)))
+        return {"tile": t.as_tuple(), "ms": b.value, "default_ms": d.value}
 
 
 def force_eval_static(params: Params, n: int, x, y, z, q, type, fx, fy, fz, stream=None) -> int:

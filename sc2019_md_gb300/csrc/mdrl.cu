@@ -4,9 +4,12 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
+#include <fstream>
 #include <map>
 #include <mutex>
 #include <set>
@@ -337,13 +340,13 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
 /* ---- kernel dispatch ---------------------------------------------------------------------- */
 
 namespace mdrl {
-force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap);
+force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap, int fw);
 force_fn pick_force_acc1(int order, bool sep, bool extra, bool wrap);
 force_fn pick_force_acc2(int order, bool sep, bool extra, bool wrap);
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap) {
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw) {
     if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_acc1(order, sep, extra, wrap);
     if (acc == MDRL_ACC_KAHAN) return pick_force_acc2(order, sep, extra, wrap);
-    return pick_force_acc0(order, sep, extra, wrap);
+    return pick_force_acc0(order, sep, extra, wrap, fw);
 }
 }  // namespace mdrl
 
@@ -355,7 +358,7 @@ mdrl_status mdrl::prepare_force_kernel(force_fn fn, int device) {
     const std::pair<const void *, int> key((const void *)fn, device);
     if (!done.count(key)) {
         MDRL_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)force_smem_bytes(MDRL_MAX_TYPES, true)));
+                                       (int)force_smem_bytes(MDRL_MAX_TYPES, true, 8)));
         done.insert(key);
     }
     return MDRL_OK;
@@ -367,13 +370,15 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
                                      unsigned long long *F64, float *F32) {
     /* the per-unit shift needs >= 4 cells on every axis; with 3 the per-pair wrap is used */
     const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
-    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap);
-    const size_t smem = force_smem_bytes(c->p.ntypes, extra);
+    const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap, fw);
+    const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
-    fn<<<units, kFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
-                                         c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr);
+    fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
+                                             c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr,
+                                             c->tile.steps_per_piece);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -785,5 +790,145 @@ extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z,
     for (int k = 0; k < 9; ++k)
         if (dst[k]) MDRL_CUDA(cudaMemcpyAsync(dst[k], src[k], fb, cudaMemcpyDeviceToHost, c->stream));
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    return MDRL_OK;
+}
+
+/* ---- tiles and the autotuner --------------------------------------------------------------- */
+
+static mdrl_status check_tile(const mdrl_tile *t, bool allow8) {
+    if (!t || (t->warps_per_cta != 4 && t->warps_per_cta != 8) || t->steps_per_piece < 1 ||
+        t->steps_per_piece > 32) {
+        set_error("tile: warps_per_cta must be 4 or 8 and steps_per_piece in 1..32");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (t->warps_per_cta == 8 && !allow8) {
+        set_error("tile: 8 warps per CTA needs MDRL_ACC_FIXED64 (and no batch)");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    return MDRL_OK;
+}
+
+static void drop_graphs(mdrl_ctx *c) {
+    for (int k = 0; k < 2; ++k) {
+        if (c->graph_exec[k]) { cudaGraphExecDestroy(c->graph_exec[k]); c->graph_exec[k] = nullptr; }
+        if (c->graph[k]) { cudaGraphDestroy(c->graph[k]); c->graph[k] = nullptr; }
+    }
+    c->graph_n = -1;
+}
+
+namespace mdrl {
+mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8) {
+    MDRL_TRY(check_tile(t, allow8));
+    if (t->warps_per_cta != c->tile.warps_per_cta || t->steps_per_piece != c->tile.steps_per_piece) {
+        MDRL_CUDA(cudaSetDevice(c->p.device));
+        if (c->stream) MDRL_CUDA(cudaStreamSynchronize(c->stream));
+        drop_graphs(c);
+        c->tile = *t;
+    }
+    return MDRL_OK;
+}
+
+/* The process-wide tuning cache, optionally backed by the file named by MDRL_TUNE_CACHE. */
+static std::mutex g_tune_mu;
+static std::map<std::string, mdrl_tile> g_tune;
+static bool g_tune_loaded = false;
+
+static void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = getenv("MDRL_TUNE_CACHE");
+    if (!path || !*path) return;
+    std::ifstream in(path);
+    std::string key;
+    int w, s;
+    float ms;
+    while (in >> key >> w >> s >> ms)
+        if ((w == 4 || w == 8) && s >= 1 && s <= 32) g_tune[key] = mdrl_tile{w, s};
+}
+
+static void tune_store_locked(const std::string &key, const mdrl_tile &t, float ms) {
+    g_tune[key] = t;
+    const char *path = getenv("MDRL_TUNE_CACHE");
+    if (!path || !*path) return;
+    std::ofstream out(path, std::ios::app);
+    out << key << ' ' << t.warps_per_cta << ' ' << t.steps_per_piece << ' ' << ms << '\n';
+}
+
+bool tune_lookup(const std::string &key, mdrl_tile *t) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    *t = it->second;
+    return true;
+}
+
+void tune_store(const std::string &key, const mdrl_tile &t, float ms) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_load_locked();
+    tune_store_locked(key, t, ms);
+}
+
+std::string tune_key_common(const mdrl_ctx *c) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "t%d-o%d-b%d-a%d-c%d-q%d-e%d", c->p.ntypes, eff_order(c), c->bins, c->p.arith,
+             c->p.accum, c->ke != 0.0f ? 1 : 0, c->p.eval);
+    return buf;
+}
+}  // namespace mdrl
+
+static const int kTuneSpp[] = {3, 4, 6, 8, 12};
+
+extern "C" mdrl_status mdrl_set_tile(mdrl_ctx *c, const mdrl_tile *t) {
+    if (!c || !t) { set_error("mdrl_set_tile: null argument"); return MDRL_ERR_INVALID_ARG; }
+    return set_tile(c, t, c->p.accum == MDRL_ACC_FIXED64);
+}
+
+extern "C" mdrl_status mdrl_get_tile(mdrl_ctx *c, mdrl_tile *t) {
+    if (!c || !t) { set_error("mdrl_get_tile: null argument"); return MDRL_ERR_INVALID_ARG; }
+    *t = c->tile;
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, float *best_ms, float *default_ms) {
+    if (!c) { set_error("mdrl_autotune: null context"); return MDRL_ERR_INVALID_ARG; }
+    if (!c->have_state) { set_error("mdrl_autotune: call mdrl_set_state first"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    char buf[96];
+    const int ppc8 = (int)std::lround(8.0 * c->n / std::max(1, c->ncells));
+    snprintf(buf, sizeof buf, "ctx-%dx%dx%d-p%d-", c->g.nc[0], c->g.nc[1], c->g.nc[2], ppc8);
+    const std::string key = std::string(buf) + tune_key_common(c);
+    auto time_tile = [&](const mdrl_tile &t, float *ms) -> mdrl_status {
+        MDRL_TRY(set_tile(c, &t, true));
+        float v[5];
+        for (int r = 0; r < 5; ++r) MDRL_TRY(mdrl_time_force(c, &v[r]));
+        std::sort(v, v + 5);
+        *ms = v[2];
+        return MDRL_OK;
+    };
+    const mdrl_tile def = {kFW, kStepsPerPiece};
+    mdrl_tile pick = def;
+    float pick_ms = 0.0f, def_ms = 0.0f;
+    const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick);
+    if (cached) {
+        MDRL_TRY(time_tile(pick, &pick_ms));
+        if (default_ms) MDRL_TRY(time_tile(def, &def_ms));
+    } else {
+        pick_ms = 3.0e38f;
+        const int nfw = c->p.accum == MDRL_ACC_FIXED64 ? 2 : 1;
+        for (int a = 0; a < nfw; ++a)
+            for (int spp : kTuneSpp) {
+                const mdrl_tile t = {a == 0 ? 4 : 8, spp};
+                float ms;
+                MDRL_TRY(time_tile(t, &ms));
+                if (t.warps_per_cta == def.warps_per_cta && t.steps_per_piece == def.steps_per_piece) def_ms = ms;
+                if (ms < pick_ms) { pick_ms = ms; pick = t; }
+            }
+        tune_store(key, pick, pick_ms);
+    }
+    MDRL_TRY(set_tile(c, &pick, true));
+    if (best) *best = pick;
+    if (best_ms) *best_ms = pick_ms;
+    if (default_ms) *default_ms = def_ms;
     return MDRL_OK;
 }

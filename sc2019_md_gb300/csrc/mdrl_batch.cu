@@ -259,9 +259,9 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
                     cost.push_back(a == c ? 0.5 * ppc * ppc : ppc * ppc);
                 }
         } else {
-            for (int b0 = 0; b0 < b.n; b0 += kFT) {
+            for (int b0 = 0; b0 < b.n; b0 += kBatchFT) {
                 items.push_back({r, b0});
-                cost.push_back((double)std::min(kFT, b.n - b0) * b.n * (b.path == kPathAllImages ? 2.0 : 1.0));
+                cost.push_back((double)std::min(kBatchFT, b.n - b0) * b.n * 2.0);
             }
         }
     }
@@ -325,11 +325,11 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
     mdrl_ctx *c = b->c;
     force_fn fn = pick_force_batch(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
-    const size_t smem = force_smem_bytes(c->p.ntypes, extra);
+    const size_t smem = force_smem_bytes(c->p.ntypes, extra, kBatchFT / 32);
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
-    fn<<<b->nitems, kFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes,
-                                             c->ke, b->ntot, F64, nullptr, c->d_cnt, c->d_unit, b->d_items,
-                                             b->d_reps);
+    fn<<<b->nitems, kBatchFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
+                                                  c->p.ntypes, c->ke, b->ntot, F64, nullptr, c->d_cnt, c->d_unit,
+                                                  b->d_items, b->d_reps, c->tile.steps_per_piece);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -598,5 +598,52 @@ extern "C" mdrl_status mdrl_batch_time_force(mdrl_batch *b, float *ms) {
     MDRL_TRY(batch_launch_force(b, c->d_pos[a], c->d_type[a], false, c->d_Fscr64));
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_CUDA(cudaEventElapsedTime(ms, c->evf0, c->evf1));
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_batch_set_tile(mdrl_batch *b, const mdrl_tile *t) {
+    if (!b || !t) { set_error("mdrl_batch_set_tile: null argument"); return MDRL_ERR_INVALID_ARG; }
+    return set_tile(b->c, t, false);
+}
+
+extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *best, float *best_ms,
+                                           float *default_ms) {
+    if (!b) { set_error("mdrl_batch_autotune: null batch"); return MDRL_ERR_INVALID_ARG; }
+    mdrl_ctx *c = b->c;
+    if (!c->have_state) { set_error("mdrl_batch_autotune: call mdrl_batch_set_state first"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    char buf[96];
+    snprintf(buf, sizeof buf, "batch-r%d-n%d-c%d-i%d-", b->nrep, b->ntot, b->ncells, b->nitems);
+    const std::string key = std::string(buf) + tune_key_common(c);
+    auto time_tile = [&](const mdrl_tile &t, float *ms) -> mdrl_status {
+        MDRL_TRY(set_tile(c, &t, false));
+        float v[5];
+        for (int r = 0; r < 5; ++r) MDRL_TRY(mdrl_batch_time_force(b, &v[r]));
+        std::sort(v, v + 5);
+        *ms = v[2];
+        return MDRL_OK;
+    };
+    const mdrl_tile def = {kBatchFT / 32, kStepsPerPiece};
+    mdrl_tile pick = def;
+    float pick_ms = 0.0f, def_ms = 0.0f;
+    const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick) && pick.warps_per_cta == 4;
+    if (cached) {
+        MDRL_TRY(time_tile(pick, &pick_ms));
+        if (default_ms) MDRL_TRY(time_tile(def, &def_ms));
+    } else {
+        pick_ms = 3.0e38f;
+        for (int spp : {3, 4, 6, 8, 12}) {
+            const mdrl_tile t = {kBatchFT / 32, spp};
+            float ms;
+            MDRL_TRY(time_tile(t, &ms));
+            if (spp == def.steps_per_piece) def_ms = ms;
+            if (ms < pick_ms) { pick_ms = ms; pick = t; }
+        }
+        tune_store(key, pick, pick_ms);
+    }
+    MDRL_TRY(set_tile(c, &pick, false));
+    if (best) *best = pick;
+    if (best_ms) *best_ms = pick_ms;
+    if (default_ms) *default_ms = def_ms;
     return MDRL_OK;
 }

@@ -103,6 +103,9 @@ struct mdrl_ctx {
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     int graph_n = -1;
     bool graph_extra = false;
+
+    /* force-kernel tile (mdrl_set_tile / mdrl_autotune) */
+    mdrl_tile tile = {mdrl::kFW, mdrl::kStepsPerPiece};
 };
 
 namespace mdrl {
@@ -113,4 +116,9 @@ mdrl_status check_device_errors(mdrl_ctx *c);
 /* Raise the dynamic shared-memory limit of a force kernel once per kernel and device. */
 mdrl_status prepare_force_kernel(force_fn fn, int device);
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
+/* Tiles: change (re-capturing graphs), and the autotuner's process-wide cache. */
+mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8);
+bool tune_lookup(const std::string &key, mdrl_tile *t);
+void tune_store(const std::string &key, const mdrl_tile &t, float ms);
+std::string tune_key_common(const mdrl_ctx *c);
 }  // namespace mdrl

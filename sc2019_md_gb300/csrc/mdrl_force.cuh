@@ -41,26 +41,35 @@ namespace mdrl {
 #ifndef MDRL_FORCE_WARPS
 #define MDRL_FORCE_WARPS 4
 #endif
-constexpr int kFW = MDRL_FORCE_WARPS;  /* warps per force CTA */
+#ifndef MDRL_STEPS_PER_PIECE
+#define MDRL_STEPS_PER_PIECE 6
+#endif
+#ifndef MDRL_FORCE_CTAS_PER_SM
+#define MDRL_FORCE_CTAS_PER_SM (16 / MDRL_FORCE_WARPS)
+#endif
+constexpr int kFW = MDRL_FORCE_WARPS;  /* default warps per force CTA (tiles may use 8) */
 constexpr int kFT = kFW * 32;
-constexpr int kStepsPerPiece = 6;      /* j-steps (of 8 particles) per piece */
+constexpr int kStepsPerPiece = MDRL_STEPS_PER_PIECE;   /* default j-steps (of 8 particles) per piece */
+constexpr int kFCtas = MDRL_FORCE_CTAS_PER_SM;         /* resident CTAs per SM the registers allow */
+constexpr int kBatchFT = 128;          /* threads of a batched-replica CTA (4 warps) */
 
 struct BatchRep;
 struct BatchItem;
 typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
                          int, float, int, unsigned long long *, float *, int *, UnitOut *,
-                         const BatchItem *, const BatchRep *);
+                         const BatchItem *, const BatchRep *, int);
 
 /* Work items (one per unit): the result slots k_totals sums. */
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
 
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap);
+/* fw: warps per CTA (8 only with int64 fixed point; otherwise 4) */
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw = kFW);
 /* the batched-replica instantiation (int64 fixed point, per-pair wrap) */
 force_fn pick_force_batch(int order, bool sep, bool extra);
 
-inline size_t force_smem_bytes(int ntypes, bool extra) {
+inline size_t force_smem_bytes(int ntypes, bool extra, int fw = kFW) {
     return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
-           sizeof(float) * kFW * 6 * kChunk + (extra ? sizeof(int) * kFW * 2 * kChunk : 0);
+           sizeof(float) * fw * 6 * kChunk + (extra ? sizeof(int) * fw * 2 * kChunk : 0);
 }
 
 /* The pair functions of an accepted pair at r2e = max(r2, 2^min_log2).  Order 1 reads one
@@ -184,7 +193,7 @@ __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32,
  *                               replica's geometry and cell offset (per-pair wrap);
  *   (replica, cell pair a <= b) every edge above 2 rc but fewer cells: the same tiled Newton-3
  *                               path over an explicit pair of cells, per-pair minimum image;
- *   (replica, kFT particles)    an edge of at most 2 rc (always above rc): every periodic image
+ *   (replica, 128 particles)    an edge of at most 2 rc (always above rc): every periodic image
  *                               within rc, all_images_body. */
 enum : int { kPathHalfShell = 0, kPathMinImage = 1, kPathAllImages = 2 };
 
@@ -208,7 +217,7 @@ struct BatchItem {
  * sums f_ij over every j != i and image, each ordered pair evaluated from i's side
  * (QQ = (ke*qi)*qj), so the particle's force is complete and is stored without atomics;
  * energies and the virial carry a factor 1/2, and pairs count j > i. */
-template <int ORDER, bool SEP, bool EXTRA>
+template <int ORDER, bool SEP, bool EXTRA, int FW>
 __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                                                    const BatchRep &rp, int b0, TableDev tab,
                                                    const float4 *sCoef, int ntypes, float ke, int ntot,
@@ -243,8 +252,8 @@ __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, 
             acc_vir += 0.5f * __fmul_rn(fs, r2);
         }
     };
-    for (int j0 = 0; j0 < rp.n; j0 += kFT) {
-        const int nj = min(kFT, rp.n - j0);
+    for (int j0 = 0; j0 < rp.n; j0 += (FW * 32)) {
+        const int nj = min((FW * 32), rp.n - j0);
         __syncthreads();
         if (tid < nj) { sJp[tid] = pos[rp.p_off + j0 + tid]; sJt[tid] = ptype[rp.p_off + j0 + tid]; }
         __syncthreads();
@@ -292,7 +301,7 @@ __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, 
 /* One unit: home-cell particles [hs, hs + ni_all) against neighbour-cell particles
  * [cs, cs + nj_all) (the same cell when self), per-unit shift (sx, sy, sz) or, with WRAP, the
  * per-pair one-wrap rule; writes the unit's totals to uout[blockIdx.x]. */
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP>
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, int FW>
 __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                                            int hs, int ni_all, int cs, int nj_all, bool self, const Geom &g,
                                            float sx, float sy, float sz, const TableDev &tab,
@@ -300,7 +309,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                                            unsigned long long *__restrict__ F64, float *__restrict__ F32,
                                            int *__restrict__ counts, UnitOut *__restrict__ uout, float4 *sIp,
                                            float4 *sJp, float4 *sCoef, int *sIt, int *sJt, float *sF, int *sC,
-                                           double (*s_red)[3], unsigned long long (*s_cnt)[2]) {
+                                           double (*s_red)[3], unsigned long long (*s_cnt)[2], int spp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
     const bool coul = ke != 0.0f;
@@ -310,7 +319,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     int *wCi = sC + warp * 2 * kChunk;
     int *wCj = wCi + kChunk;
 
-    for (int t = tid; t < ntypes * ntypes; t += kFT) sCoef[t] = pcoef[t];
+    for (int t = tid; t < ntypes * ntypes; t += (FW * 32)) sCoef[t] = pcoef[t];
 
     float acc_elj = 0.0f, acc_ec = 0.0f, acc_vir = 0.0f;
     unsigned acc_pairs = 0, acc_below = 0;
@@ -320,37 +329,37 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
             const int ni = min(kChunk, ni_all - i0), nj = min(kChunk, nj_all - j0);
             const bool diag = self && (i0 == j0);
             __syncthreads();
-            for (int t = tid; t < ni; t += kFT) {
+            for (int t = tid; t < ni; t += (FW * 32)) {
                 sIp[t] = pos[hs + i0 + t];
                 sIt[t] = ptype[hs + i0 + t] * ntypes;
             }
-            for (int t = tid; t < nj; t += kFT) {
+            for (int t = tid; t < nj; t += (FW * 32)) {
                 sJp[t] = pos[cs + j0 + t];
                 sJt[t] = ptype[cs + j0 + t];
             }
-            for (int t = tid; t < kFW * 6 * kChunk; t += kFT) sF[t] = 0.0f;
+            for (int t = tid; t < FW * 6 * kChunk; t += (FW * 32)) sF[t] = 0.0f;
             if (EXTRA)
-                for (int t = tid; t < kFW * 2 * kChunk; t += kFT) sC[t] = 0;
+                for (int t = tid; t < FW * 2 * kChunk; t += (FW * 32)) sC[t] = 0;
             __syncthreads();
 
             const int nti = (ni + 31) >> 5;
             const int S = (nj + 7) >> 3;                         /* j-steps of 8 */
-            /* pieces: tile ti covers steps [first(ti), S) in runs of kStepsPerPiece */
+            /* pieces: tile ti covers steps [first(ti), S) in runs of spp */
             int npieces = 0;
             for (int ti = 0; ti < nti; ++ti) {
                 const int first = diag ? 4 * ti : 0;
-                npieces += (S - first + kStepsPerPiece - 1) / kStepsPerPiece;
+                npieces += (S - first + spp - 1) / spp;
             }
-            for (int p = warp; p < npieces; p += kFW) {
+            for (int p = warp; p < npieces; p += FW) {
                 int ti = 0, r = p, first = 0, cnt = 0;
                 for (;; ++ti) {
                     first = diag ? 4 * ti : 0;
-                    cnt = (S - first + kStepsPerPiece - 1) / kStepsPerPiece;
+                    cnt = (S - first + spp - 1) / spp;
                     if (r < cnt) break;
                     r -= cnt;
                 }
-                const int s0 = first + r * kStepsPerPiece;
-                const int s1 = min(S, s0 + kStepsPerPiece);
+                const int s0 = first + r * spp;
+                const int s1 = min(S, s0 + spp);
                 float xi[8], yi[8], zi[8], qi[8];
                 int tti[8];
 #pragma unroll
@@ -460,11 +469,11 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
             }
             __syncthreads();
             /* sum the warp accumulators in warp order; one atomic per particle and component */
-            for (int t = tid; t < ni; t += kFT) {
+            for (int t = tid; t < ni; t += (FW * 32)) {
                 float v0 = 0.f, v1 = 0.f, v2 = 0.f;
                 int cc = 0;
 #pragma unroll
-                for (int w = 0; w < kFW; ++w) {
+                for (int w = 0; w < FW; ++w) {
                     const float *a = sF + w * 6 * kChunk;
                     v0 += a[t]; v1 += a[kChunk + t]; v2 += a[2 * kChunk + t];
                     if (diag) { v0 += a[3 * kChunk + t]; v1 += a[4 * kChunk + t]; v2 += a[5 * kChunk + t]; }
@@ -474,11 +483,11 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                 if (EXTRA && cc) atomicAdd(counts + hs + i0 + t, cc);
             }
             if (!diag) {
-                for (int t = tid; t < nj; t += kFT) {
+                for (int t = tid; t < nj; t += (FW * 32)) {
                     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
                     int cc = 0;
 #pragma unroll
-                    for (int w = 0; w < kFW; ++w) {
+                    for (int w = 0; w < FW; ++w) {
                         const float *a = sF + w * 6 * kChunk + 3 * kChunk;
                         v0 += a[t]; v1 += a[kChunk + t]; v2 += a[2 * kChunk + t];
                         if (EXTRA) cc += sC[w * 2 * kChunk + kChunk + t];
@@ -511,7 +520,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
         UnitOut u;
         u.e_lj = u.e_coul = u.virial = 0.0;
         u.pairs = u.below = 0ull;
-        for (int w = 0; w < kFW; ++w) {
+        for (int w = 0; w < FW; ++w) {
             u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
             u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
         }
@@ -519,23 +528,23 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     }
 }
 
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false>
-__global__ void __launch_bounds__(kFT, 16 / kFW)
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false, int FW = kFW>
+__global__ void __launch_bounds__(FW * 32, (FW == kFW ? kFCtas : 16 / FW))
 k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         const int *__restrict__ cstart, Geom gparam, TableDev tab, const float4 *__restrict__ pcoef,
         int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
         float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout,
-        const BatchItem *__restrict__ items = nullptr, const BatchRep *__restrict__ reps = nullptr) {
+        const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int spp) {
     extern __shared__ float4 smem[];
     float4 *sIp = smem;
     float4 *sJp = sIp + kChunk;
     float4 *sCoef = sJp + kChunk;
     int *sIt = reinterpret_cast<int *>(sCoef + ntypes * ntypes);
     int *sJt = sIt + kChunk;
-    float *sF = reinterpret_cast<float *>(sJt + kChunk);             /* [kFW][2][3][kChunk] */
-    int *sC = reinterpret_cast<int *>(sF + kFW * 6 * kChunk);       /* [kFW][2][kChunk] */
-    __shared__ double s_red[kFW][3];
-    __shared__ unsigned long long s_cnt[kFW][2];
+    float *sF = reinterpret_cast<float *>(sJt + kChunk);             /* [FW][2][3][kChunk] */
+    int *sC = reinterpret_cast<int *>(sF + FW * 6 * kChunk);       /* [FW][2][kChunk] */
+    __shared__ double s_red[FW][3];
+    __shared__ unsigned long long s_cnt[FW][2];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
@@ -546,10 +555,10 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         const BatchItem it = items[blockIdx.x];
         const BatchRep rp = reps[it.rep];
         if (rp.path == kPathAllImages) {
-            for (int t = tid; t < ntypes * ntypes; t += kFT) sCoef[t] = pcoef[t];
+            for (int t = tid; t < ntypes * ntypes; t += (FW * 32)) sCoef[t] = pcoef[t];
             float e1 = 0.f, e2 = 0.f, e3 = 0.f;
             unsigned c1 = 0, c2 = 0;
-            all_images_body<ORDER, SEP, EXTRA>(pos, ptype, rp, it.unit, tab, sCoef, ntypes, ke, n, F64, counts,
+            all_images_body<ORDER, SEP, EXTRA, FW>(pos, ptype, rp, it.unit, tab, sCoef, ntypes, ke, n, F64, counts,
                                                   sJp, sJt, e1, e2, e3, c1, c2);
             double d1 = e1, d2 = e2, d3 = e3;
             unsigned long long u1 = c1, u2 = c2;
@@ -572,7 +581,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                 UnitOut u;
                 u.e_lj = u.e_coul = u.virial = 0.0;
                 u.pairs = u.below = 0ull;
-                for (int w = 0; w < kFW; ++w) {
+                for (int w = 0; w < FW; ++w) {
                     u.e_lj += s_red[w][0]; u.e_coul += s_red[w][1]; u.virial += s_red[w][2];
                     u.pairs += s_cnt[w][0]; u.below += s_cnt[w][1];
                 }
@@ -617,17 +626,17 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
     if constexpr (BATCH) {
         if (use_wrap)
-            force_unit<ORDER, SEP, EXTRA, ACC, true>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+            force_unit<ORDER, SEP, EXTRA, ACC, true, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
                                                      pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
-                                                     sCoef, sIt, sJt, sF, sC, s_red, s_cnt);
+                                                     sCoef, sIt, sJt, sF, sC, s_red, s_cnt, spp);
         else
-            force_unit<ORDER, SEP, EXTRA, ACC, false>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+            force_unit<ORDER, SEP, EXTRA, ACC, false, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
                                                       pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
-                                                      sCoef, sIt, sJt, sF, sC, s_red, s_cnt);
+                                                      sCoef, sIt, sJt, sF, sC, s_red, s_cnt, spp);
     } else {
-        force_unit<ORDER, SEP, EXTRA, ACC, WRAP>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
+        force_unit<ORDER, SEP, EXTRA, ACC, WRAP, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
                                                  pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp, sCoef,
-                                                 sIt, sJt, sF, sC, s_red, s_cnt);
+                                                 sIt, sJt, sF, sC, s_red, s_cnt, spp);
     }
 }
 

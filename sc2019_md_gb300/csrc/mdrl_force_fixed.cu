@@ -7,32 +7,39 @@
 
 namespace mdrl {
 
-template <int ORDER, bool SEP, bool EXTRA>
+template <int ORDER, bool SEP, bool EXTRA, int FW>
 static force_fn pick_wrap_0(bool wrap) {
-    return wrap ? (force_fn)k_force<ORDER, SEP, EXTRA, 0, true> : (force_fn)k_force<ORDER, SEP, EXTRA, 0, false>;
+    return wrap ? (force_fn)k_force<ORDER, SEP, EXTRA, 0, true, false, FW>
+                : (force_fn)k_force<ORDER, SEP, EXTRA, 0, false, false, FW>;
 }
 
-template <int ORDER>
+template <int ORDER, int FW>
 static force_fn pick_order_0(bool sep, bool extra, bool wrap) {
-    if (sep) return extra ? pick_wrap_0<ORDER, true, true>(wrap) : pick_wrap_0<ORDER, true, false>(wrap);
-    return extra ? pick_wrap_0<ORDER, false, true>(wrap) : pick_wrap_0<ORDER, false, false>(wrap);
+    if (sep) return extra ? pick_wrap_0<ORDER, true, true, FW>(wrap) : pick_wrap_0<ORDER, true, false, FW>(wrap);
+    return extra ? pick_wrap_0<ORDER, false, true, FW>(wrap) : pick_wrap_0<ORDER, false, false, FW>(wrap);
 }
 
-force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap) {
+template <int FW>
+static force_fn pick_fw_0(int order, bool sep, bool extra, bool wrap) {
     switch (order) {
-        case 0: return pick_order_0<0>(sep, extra, wrap);
-        case 1: return pick_order_0<1>(sep, extra, wrap);
-        case 2: return pick_order_0<2>(sep, extra, wrap);
-        default: return pick_order_0<3>(sep, extra, wrap);
+        case 0: return pick_order_0<0, FW>(sep, extra, wrap);
+        case 1: return pick_order_0<1, FW>(sep, extra, wrap);
+        case 2: return pick_order_0<2, FW>(sep, extra, wrap);
+        default: return pick_order_0<3, FW>(sep, extra, wrap);
     }
+}
+
+/* Fixed point is the tuned mode: CTAs of 4 or 8 warps. */
+force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap, int fw) {
+    return fw == 8 ? pick_fw_0<8>(order, sep, extra, wrap) : pick_fw_0<4>(order, sep, extra, wrap);
 }
 
 template <int ORDER>
 static force_fn pick_batch_order(bool sep, bool extra) {
-    if (sep) return extra ? (force_fn)k_force<ORDER, true, true, 0, true, true>
-                          : (force_fn)k_force<ORDER, true, false, 0, true, true>;
-    return extra ? (force_fn)k_force<ORDER, false, true, 0, true, true>
-                 : (force_fn)k_force<ORDER, false, false, 0, true, true>;
+    if (sep) return extra ? (force_fn)k_force<ORDER, true, true, 0, true, true, kBatchFT / 32>
+                          : (force_fn)k_force<ORDER, true, false, 0, true, true, kBatchFT / 32>;
+    return extra ? (force_fn)k_force<ORDER, false, true, 0, true, true, kBatchFT / 32>
+                 : (force_fn)k_force<ORDER, false, false, 0, true, true, kBatchFT / 32>;
 }
 
 force_fn pick_force_batch(int order, bool sep, bool extra) {

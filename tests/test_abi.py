@@ -38,7 +38,8 @@ def test_struct_layouts_match_header():
     """Field order and count of mdrl_params / mdrl_stats / mdrl_replica in the header equal the
     mirror's."""
     text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "mdrl.h").read_text(), flags=re.S)
-    for cname, cls in (("mdrl_params", m.Params), ("mdrl_stats", m.Stats), ("mdrl_replica", m.Replica)):
+    for cname, cls in (("mdrl_params", m.Params), ("mdrl_stats", m.Stats), ("mdrl_replica", m.Replica),
+                       ("mdrl_tile", m.Tile)):
         body = re.search(r"typedef struct \{((?:(?!typedef struct).)*?)\}\s*" + cname + ";", text, re.S).group(1)
         fields = []
         for decl in body.split(";"):
