@@ -160,6 +160,12 @@ mdrl_status mdrl_get_tables(mdrl_ctx *ctx, int *order, int *nseg, int *bins, int
  * B6 = -4*eps*sig^6, Lorentz-Berthelot mixing). */
 mdrl_status mdrl_get_pair_coefficients(mdrl_ctx *ctx, float *coef);
 
+/* Replace the per-type-pair multipliers (no counterpart in the reference, whose single LJ type
+ * is baked into its tables): coef[ntypes*ntypes*4] = A14, B8, A12, B6 in FP64 (stored as FP32),
+ * e.g. from an Amber topology's E = A/r^12 - B/r^6: A14 = 12A, B8 = -6B, A12 = A, B6 = -B.
+ * The matrix should be symmetric for Newton's third law to hold. */
+mdrl_status mdrl_set_pair_coefficients(mdrl_ctx *ctx, const double *coef);
+
 /* Cell-list binning only (host arrays).  cell_of[n]: cell of each particle,
  * (cx*ny + cy)*nz + cz with c = floor(x / (box/ncell)); cell_count[ncells]; order[n]: particle
  * ids cell by cell, each cell in input order.  Any output may be NULL. */
@@ -259,6 +265,8 @@ mdrl_status mdrl_batch_get_state(mdrl_batch *batch, float *x, float *y, float *z
 mdrl_status mdrl_batch_replica_stats(mdrl_batch *batch, mdrl_stats *out);
 /* Device time of one force launch over the whole batch (see mdrl_time_force). */
 mdrl_status mdrl_batch_time_force(mdrl_batch *batch, float *ms);
+/* See mdrl_set_pair_coefficients. */
+mdrl_status mdrl_batch_set_pair_coefficients(mdrl_batch *batch, const double *coef);
 
 /* ---- tiles and the autotuner ---------------------------------------------------------------
  * No counterpart in the reference.  mdrl_autotune times the force kernel (mdrl_time_force's

@@ -73,6 +73,7 @@ class Stats(C.Structure):
 
 _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int)
+_D = C.POINTER(C.c_double)
 _lib = None
 
 
@@ -136,12 +137,14 @@ def lib() -> C.CDLL:
     L.mdrl_batch_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
     L.mdrl_batch_replica_stats.argtypes = [vp, C.POINTER(Stats)]
     L.mdrl_batch_time_force.argtypes = [vp, _F]
+    L.mdrl_set_pair_coefficients.argtypes = [vp, _D]
+    L.mdrl_batch_set_pair_coefficients.argtypes = [vp, _D]
     L.mdrl_set_tile.argtypes = [vp, C.POINTER(Tile)]
     L.mdrl_get_tile.argtypes = [vp, C.POINTER(Tile)]
     L.mdrl_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
     L.mdrl_batch_set_tile.argtypes = [vp, C.POINTER(Tile)]
     L.mdrl_batch_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
-    for name in ("mdrl_set_tile", "mdrl_get_tile", "mdrl_autotune", "mdrl_batch_set_tile", "mdrl_batch_autotune",
+    for name in ("mdrl_set_pair_coefficients", "mdrl_batch_set_pair_coefficients", "mdrl_set_tile", "mdrl_get_tile", "mdrl_autotune", "mdrl_batch_set_tile", "mdrl_batch_autotune",
                  "mdrl_batch_create", "mdrl_batch_destroy", "mdrl_batch_layout", "mdrl_batch_force_eval",
                  "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
                  "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
@@ -246,6 +249,13 @@ class Context:
         coef = np.ascontiguousarray(coef, dtype=np.float32)
         nfunc = coef.shape[0]
         _check(lib().mdrl_set_tables(self._h, order, nseg, bins, min_log2, nfunc, _fp(coef), int(raw)))
+
+    def set_pair_coefficients(self, coef) -> None:
+        """Per-type-pair multipliers (ntypes*ntypes, 4): A14, B8, A12, B6 (FP64)."""
+        c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1)
+        if c.size != self.params.ntypes ** 2 * 4:
+            raise ValueError("coef must hold ntypes*ntypes*4 values")
+        _check(lib().mdrl_set_pair_coefficients(self._h, c.ctypes.data_as(_D)))
 
     def pair_coefficients(self) -> np.ndarray:
         T = self.params.ntypes
@@ -432,6 +442,12 @@ class Batch:
     def set_tile(self, warps_per_cta: int, steps_per_piece: int) -> None:
         t = Tile(warps_per_cta, steps_per_piece)
         _check(lib().mdrl_batch_set_tile(self._h, C.byref(t)))
+
+    def set_pair_coefficients(self, coef) -> None:
+        c = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1)
+        if c.size != self.params.ntypes ** 2 * 4:
+            raise ValueError("coef must hold ntypes*ntypes*4 values")
+        _check(lib().mdrl_batch_set_pair_coefficients(self._h, c.ctypes.data_as(_D)))
 
     def autotune(self, retime: bool = False) -> dict:
         t, b, d = Tile(), C.c_float(), C.c_float()

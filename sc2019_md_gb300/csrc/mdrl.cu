@@ -591,6 +591,26 @@ extern "C" mdrl_status mdrl_get_pair_coefficients(mdrl_ctx *c, float *coef) {
     return MDRL_OK;
 }
 
+extern "C" mdrl_status mdrl_set_pair_coefficients(mdrl_ctx *c, const double *coef) {
+    if (!c || !coef) { set_error("mdrl_set_pair_coefficients: null argument"); return MDRL_ERR_INVALID_ARG; }
+    const int T = c->p.ntypes;
+    std::vector<float> pc((size_t)T * T * 4);
+    for (size_t k = 0; k < pc.size(); ++k) {
+        if (!std::isfinite(coef[k]) || std::fabs(coef[k]) > 3.0e38) {
+            set_error("mdrl_set_pair_coefficients: coefficients must be finite FP32 values");
+            return MDRL_ERR_INVALID_ARG;
+        }
+        pc[k] = (float)coef[k];
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    if (c->stream) MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    c->pcoef = pc;
+    c->raw = false;
+    /* same size and address: captured step graphs stay valid */
+    MDRL_CUDA(cudaMemcpy(c->d_pcoef, pc.data(), sizeof(float) * pc.size(), cudaMemcpyHostToDevice));
+    return MDRL_OK;
+}
+
 extern "C" mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples,
                                        float *coef) {
     if (!coef || order < 1 || order > 3 || nseg < 1 || bins < 1 || samples < order + 1 || samples > 1024) {

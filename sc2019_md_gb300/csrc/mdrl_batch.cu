@@ -647,3 +647,8 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
     if (default_ms) *default_ms = def_ms;
     return MDRL_OK;
 }
+
+extern "C" mdrl_status mdrl_batch_set_pair_coefficients(mdrl_batch *b, const double *coef) {
+    if (!b) { set_error("mdrl_batch_set_pair_coefficients: null batch"); return MDRL_ERR_INVALID_ARG; }
+    return mdrl_set_pair_coefficients(b->c, coef);
+}

@@ -29,26 +29,12 @@ static force_fn pick_fw_0(int order, bool sep, bool extra, bool wrap) {
     }
 }
 
+/* The 8-warp instantiations compile in their own translation unit (mdrl_force_fixed8.cu). */
+force_fn pick_force_acc0_w8(int order, bool sep, bool extra, bool wrap);
+
 /* Fixed point is the tuned mode: CTAs of 4 or 8 warps. */
 force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap, int fw) {
-    return fw == 8 ? pick_fw_0<8>(order, sep, extra, wrap) : pick_fw_0<4>(order, sep, extra, wrap);
-}
-
-template <int ORDER>
-static force_fn pick_batch_order(bool sep, bool extra) {
-    if (sep) return extra ? (force_fn)k_force<ORDER, true, true, 0, true, true, kBatchFT / 32>
-                          : (force_fn)k_force<ORDER, true, false, 0, true, true, kBatchFT / 32>;
-    return extra ? (force_fn)k_force<ORDER, false, true, 0, true, true, kBatchFT / 32>
-                 : (force_fn)k_force<ORDER, false, false, 0, true, true, kBatchFT / 32>;
-}
-
-force_fn pick_force_batch(int order, bool sep, bool extra) {
-    switch (order) {
-        case 0: return pick_batch_order<0>(sep, extra);
-        case 1: return pick_batch_order<1>(sep, extra);
-        case 2: return pick_batch_order<2>(sep, extra);
-        default: return pick_batch_order<3>(sep, extra);
-    }
+    return fw == 8 ? pick_force_acc0_w8(order, sep, extra, wrap) : pick_fw_0<4>(order, sep, extra, wrap);
 }
 
 }  // namespace mdrl

@@ -16,6 +16,14 @@ except the .npz/.txt files it writes.
                    sigma 2.1, eps 1.995996^2, 9 segments x 256 bins from 2^-2)
   cmodel_*.txt     a seeded 500-atom argon PDB and the stdout of the unmodified reference C model
                    run on it (100 iterations)
+  cell_images_20k.json  SHA-256 and particle count of the 64 RTL cell-memory images
+                   MatlabScripts/cell_ini_file_gen/cell_ini_file_{1..4}_{1..4}_{1..4}.{mif,hex}
+                   (built by the reference from the same 20k positions, 7 x 6 x 6 cells of 8.5 A)
+  amber_dhfr.json  a digest of MatlabScripts/DHFR_23k_Input_Dataset/{prmtop,inpcrd}: file SHA-256,
+                   pointers, box, net charge, the first atoms' fields and the 16 x 16 LJ A / B
+                   (checked by the readers' tests when the reference tree is present)
+
+Select fixtures by name on the command line (default: all).
 """
 from __future__ import annotations
 
@@ -144,10 +152,51 @@ def cmodel() -> None:
     print("cmodel:", res.stdout.splitlines()[-1])
 
 
+def cell_images() -> None:
+    import hashlib
+    import json
+    out = {}
+    for x in range(1, 5):
+        for y in range(1, 5):
+            for z in range(1, 5):
+                base = MS / "cell_ini_file_gen" / f"cell_ini_file_{x}_{y}_{z}"
+                mif = base.with_suffix(".mif").read_bytes()
+                count = int(re.search(rb"\n0 : ([0-9A-F]{24});", mif).group(1), 16)
+                out[f"{x}_{y}_{z}"] = {"count": count,
+                                       "mif": hashlib.sha256(mif).hexdigest(),
+                                       "hex": hashlib.sha256(base.with_suffix(".hex").read_bytes()).hexdigest()}
+    (HERE / "cell_images_20k.json").write_text(json.dumps(out, indent=0, sort_keys=True) + "\n")
+    print("cell_images:", len(out), "cells")
+
+
+def amber() -> None:
+    import hashlib
+    import json
+    sys.path.insert(0, str(REPO))
+    from sc2019_md_gb300 import formats
+    d = MS / "DHFR_23k_Input_Dataset"
+    prm = formats.read_amber_prmtop(d / "prmtop")
+    crd = formats.read_amber_inpcrd(d / "inpcrd")
+    nb = formats.amber_nonbonded(prm)
+    out = {"prmtop_sha256": hashlib.sha256((d / "prmtop").read_bytes()).hexdigest(),
+           "inpcrd_sha256": hashlib.sha256((d / "inpcrd").read_bytes()).hexdigest(),
+           "pointers": prm["POINTERS"], "box": [float(v) for v in crd["box"]],
+           "net_charge_e": float(nb["charge"].sum()), "mass_total": float(nb["mass"].sum()),
+           "first_atoms": [{"name": prm["ATOM_NAME"][i], "charge_e": float(nb["charge"][i]),
+                            "type": int(nb["type"][i]), "mass": float(nb["mass"][i]),
+                            "pos": [float(v) for v in crd["pos"][i]], "vel": [float(v) for v in crd["vel"][i]]}
+                           for i in range(3)],
+           "residues_first": prm["RESIDUE_LABEL"][:5],
+           "A": nb["A"].tolist(), "B": nb["B"].tolist()}
+    (HERE / "amber_dhfr.json").write_text(json.dumps(out, indent=0) + "\n")
+    print("amber:", out["pointers"]["NATOM"], "atoms")
+
+
+FIXTURES = {"kat1": kat1, "kat2": kat2, "kat3": kat3, "cmodel": cmodel, "cell_images": cell_images,
+            "amber": amber}
+
 if __name__ == "__main__":
     if not MS.exists():
         sys.exit(f"reference tree not found at {REF}")
-    kat1()
-    kat2()
-    kat3()
-    cmodel()
+    for name in (sys.argv[1:] or list(FIXTURES)):
+        FIXTURES[name]()
