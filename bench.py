@@ -399,7 +399,8 @@ def run_batch(args, rank, world, local, dist):
                        "ms_per_step": one_ms / k1,
                        "how": "a batch of one replica each (default tile), stepped in turn, each its own graph"},
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak, "kernel": "k_force (batched work list)",
+                     "frac": achieved_tf / fp32_peak, "traffic": committed_traffic("batch512"),
+                     "kernel": "k_force (batched work list)",
                      "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR},
         "gpu_launches": 9 * args.steps,
         "clocks": clk,
