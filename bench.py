@@ -293,12 +293,13 @@ def run_ours(args, rank, world, local, dist):
         "config": {"workload": workload_desc(sysm, params.table_order, params.table_bins),
                    "accumulation": "int64 fixed point 2^-24 (tuned)", "parallelism": f"replicas x{world}",
                    "tile": {"warps_per_cta": tune["tile"][0], "steps_per_piece": tune["tile"][1],
+                            "prune_steps": tune["tile"][2],
                             "autotuned": not args.no_tune, "force_ms_tuned": tune["ms"],
                             "force_ms_default_tile": tune["default_ms"]},
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
                    "pairs_per_step": pairs_launch},
         "plain": {"value": float(psum[2]) / (float(emax[1]) * 1e-3), "unit": "pair-evals/s",
-                  "ms_per_step": float(emax[1]) / kp, "accumulation": "FP32 atomics, default tile (4 warps, 6 steps)",
+                  "ms_per_step": float(emax[1]) / kp, "accumulation": "FP32 atomics, default tile (4 warps, 6 steps, no pruning)",
                   "steps": kp,
                   "force_ms": float(np.mean(pfms))},
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -342,7 +343,7 @@ def run_batch(args, rank, world, local, dist):
     b = m.Batch(params, spec)
     lay = b.layout()
     b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
-    tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6), "ms": None, "default_ms": None}
+    tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6, 0), "ms": None, "default_ms": None}
     b.step(args.warmup)
     torch.cuda.synchronize()
     clocks = Clocks(local)
@@ -391,7 +392,8 @@ def run_batch(args, rank, world, local, dist):
                                f"{args.bins}-bin tables, int64 fixed point, velocity Verlet 2 fs",
                    "paths": {"half_shell": int(npath[0]), "min_image": int(npath[1]), "all_images": int(npath[2])},
                    "work_items": int(lay["total_items"]), "pairs_per_step": float(np.mean(pstep)),
-                   "tile": {"steps_per_piece": tune["tile"][1], "autotuned": not args.no_tune,
+                   "tile": {"steps_per_piece": tune["tile"][1], "prune_steps": tune["tile"][2],
+                            "autotuned": not args.no_tune,
                             "force_ms_tuned": tune["ms"], "force_ms_default_tile": tune["default_ms"]},
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
                    "generation_s": gen_s},

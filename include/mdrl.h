@@ -116,10 +116,13 @@ typedef struct {
 typedef struct mdrl_ctx mdrl_ctx;
 
 /* Tile of the half-shell force kernel: warps per CTA (4, or 8 with MDRL_ACC_FIXED64 outside a
- * batch) and j-steps of 8 particles per work piece (1..32).  Default {4, 6}. */
+ * batch), j-steps of 8 particles per work piece (1..32), and whether a unit first drops the
+ * (32-i, 8-j) blocks whose bounding boxes are beyond rc (exact; pays with many particles per
+ * cell or cells well above rc).  Default {4, 6, 0}. */
 typedef struct {
     int warps_per_cta;
     int steps_per_piece;
+    int prune_steps;
 } mdrl_tile;
 
 /* Library identity and the last error text of the calling thread ("" when none). */
@@ -273,7 +276,7 @@ mdrl_status mdrl_batch_set_pair_coefficients(mdrl_batch *batch, const double *co
  * launch, median of 5) for every candidate tile on the context's current state (call it after
  * mdrl_set_state), keeps the fastest and returns it with its time and the default tile's time.
  * Candidates: warps per CTA {4, 8} (8 with MDRL_ACC_FIXED64 only) x steps per piece
- * {3, 4, 6, 8, 12}.  Results are cached per process under a key of the cell grid, mean cell
+ * {3, 4, 6, 8, 12} x pruning {off, on}.  Results are cached per process under a key of the cell grid, mean cell
  * occupancy (to 1/8), types, table order and bins, arithmetic, accumulation and Coulomb on/off;
  * a cached key is reused without timing unless flags has MDRL_TUNE_RETIME.  When the environment
  * variable MDRL_TUNE_CACHE names a file, results are appended to it and read back by later
@@ -282,7 +285,8 @@ mdrl_status mdrl_batch_set_pair_coefficients(mdrl_batch *batch, const double *co
 mdrl_status mdrl_set_tile(mdrl_ctx *ctx, const mdrl_tile *tile);
 mdrl_status mdrl_get_tile(mdrl_ctx *ctx, mdrl_tile *tile);
 mdrl_status mdrl_autotune(mdrl_ctx *ctx, int flags, mdrl_tile *best, float *best_ms, float *default_ms);
-/* The same for a batch (4 warps per CTA; steps per piece tuned), after mdrl_batch_set_state. */
+/* The same for a batch (4 warps per CTA; steps per piece and pruning tuned), after
+ * mdrl_batch_set_state. */
 mdrl_status mdrl_batch_set_tile(mdrl_batch *batch, const mdrl_tile *tile);
 mdrl_status mdrl_batch_autotune(mdrl_batch *batch, int flags, mdrl_tile *best, float *best_ms,
                                 float *default_ms);

@@ -78,10 +78,10 @@ _lib = None
 
 
 class Tile(C.Structure):
-    _fields_ = [("warps_per_cta", C.c_int), ("steps_per_piece", C.c_int)]
+    _fields_ = [("warps_per_cta", C.c_int), ("steps_per_piece", C.c_int), ("prune_steps", C.c_int)]
 
     def as_tuple(self):
-        return (self.warps_per_cta, self.steps_per_piece)
+        return (self.warps_per_cta, self.steps_per_piece, self.prune_steps)
 
 
 TUNE_RETIME = 1
@@ -333,8 +333,8 @@ class Context:
         _check(lib().mdrl_time_force(self._h, C.byref(ms)))
         return ms.value
 
-    def set_tile(self, warps_per_cta: int, steps_per_piece: int) -> None:
-        t = Tile(warps_per_cta, steps_per_piece)
+    def set_tile(self, warps_per_cta: int, steps_per_piece: int, prune_steps: int = 0) -> None:
+        t = Tile(warps_per_cta, steps_per_piece, prune_steps)
         _check(lib().mdrl_set_tile(self._h, C.byref(t)))
 
     def tile(self) -> tuple:
@@ -439,8 +439,8 @@ class Batch:
         _check(lib().mdrl_batch_time_force(self._h, C.byref(ms)))
         return ms.value
 
-    def set_tile(self, warps_per_cta: int, steps_per_piece: int) -> None:
-        t = Tile(warps_per_cta, steps_per_piece)
+    def set_tile(self, warps_per_cta: int, steps_per_piece: int, prune_steps: int = 0) -> None:
+        t = Tile(warps_per_cta, steps_per_piece, prune_steps)
         _check(lib().mdrl_batch_set_tile(self._h, C.byref(t)))
 
     def set_pair_coefficients(self, coef) -> None:

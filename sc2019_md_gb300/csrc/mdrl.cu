@@ -340,13 +340,17 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
 /* ---- kernel dispatch ---------------------------------------------------------------------- */
 
 namespace mdrl {
-force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap, int fw);
-force_fn pick_force_acc1(int order, bool sep, bool extra, bool wrap);
-force_fn pick_force_acc2(int order, bool sep, bool extra, bool wrap);
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw) {
-    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_acc1(order, sep, extra, wrap);
-    if (acc == MDRL_ACC_KAHAN) return pick_force_acc2(order, sep, extra, wrap);
-    return pick_force_acc0(order, sep, extra, wrap, fw);
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw, bool prune) {
+    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false>(order, sep, extra, wrap);
+    if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false>(order, sep, extra, wrap);
+    if (fw == 8) return prune ? pick_force_set<0, 8, true>(order, sep, extra, wrap)
+                              : pick_force_set<0, 8, false>(order, sep, extra, wrap);
+    return prune ? pick_force_set<0, 4, true>(order, sep, extra, wrap)
+                 : pick_force_set<0, 4, false>(order, sep, extra, wrap);
+}
+
+force_fn pick_force_batch(int order, bool sep, bool extra, bool prune) {
+    return prune ? pick_batch_set<true>(order, sep, extra) : pick_batch_set<false>(order, sep, extra);
 }
 }  // namespace mdrl
 
@@ -371,14 +375,15 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
     /* the per-unit shift needs >= 4 cells on every axis; with 3 the per-pair wrap is used */
     const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
     const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
-    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap, fw);
+    const bool prune = c->p.accum == MDRL_ACC_FIXED64 && c->tile.prune_steps;
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap, fw, prune);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
                                              c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr,
-                                             c->tile.steps_per_piece);
+                                             tile_word(c->tile.steps_per_piece, c->tile.prune_steps));
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -815,14 +820,18 @@ extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z,
 
 /* ---- tiles and the autotuner --------------------------------------------------------------- */
 
-static mdrl_status check_tile(const mdrl_tile *t, bool allow8) {
+static mdrl_status check_tile(const mdrl_tile *t, bool allow8, bool allow_prune) {
     if (!t || (t->warps_per_cta != 4 && t->warps_per_cta != 8) || t->steps_per_piece < 1 ||
-        t->steps_per_piece > 32) {
-        set_error("tile: warps_per_cta must be 4 or 8 and steps_per_piece in 1..32");
+        t->steps_per_piece > 32 || (t->prune_steps != 0 && t->prune_steps != 1)) {
+        set_error("tile: warps_per_cta must be 4 or 8, steps_per_piece in 1..32, prune_steps 0 or 1");
         return MDRL_ERR_INVALID_ARG;
     }
     if (t->warps_per_cta == 8 && !allow8) {
         set_error("tile: 8 warps per CTA needs MDRL_ACC_FIXED64 (and no batch)");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (t->prune_steps && !allow_prune) {
+        set_error("tile: pruning needs MDRL_ACC_FIXED64");
         return MDRL_ERR_INVALID_ARG;
     }
     return MDRL_OK;
@@ -838,8 +847,9 @@ static void drop_graphs(mdrl_ctx *c) {
 
 namespace mdrl {
 mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8) {
-    MDRL_TRY(check_tile(t, allow8));
-    if (t->warps_per_cta != c->tile.warps_per_cta || t->steps_per_piece != c->tile.steps_per_piece) {
+    MDRL_TRY(check_tile(t, allow8, c->p.accum == MDRL_ACC_FIXED64));
+    if (t->warps_per_cta != c->tile.warps_per_cta || t->steps_per_piece != c->tile.steps_per_piece ||
+        t->prune_steps != c->tile.prune_steps) {
         MDRL_CUDA(cudaSetDevice(c->p.device));
         if (c->stream) MDRL_CUDA(cudaStreamSynchronize(c->stream));
         drop_graphs(c);
@@ -860,10 +870,10 @@ static void tune_load_locked() {
     if (!path || !*path) return;
     std::ifstream in(path);
     std::string key;
-    int w, s;
+    int w, s, pr;
     float ms;
-    while (in >> key >> w >> s >> ms)
-        if ((w == 4 || w == 8) && s >= 1 && s <= 32) g_tune[key] = mdrl_tile{w, s};
+    while (in >> key >> w >> s >> pr >> ms)
+        if ((w == 4 || w == 8) && s >= 1 && s <= 32 && (pr == 0 || pr == 1)) g_tune[key] = mdrl_tile{w, s, pr};
 }
 
 static void tune_store_locked(const std::string &key, const mdrl_tile &t, float ms) {
@@ -871,7 +881,7 @@ static void tune_store_locked(const std::string &key, const mdrl_tile &t, float 
     const char *path = getenv("MDRL_TUNE_CACHE");
     if (!path || !*path) return;
     std::ofstream out(path, std::ios::app);
-    out << key << ' ' << t.warps_per_cta << ' ' << t.steps_per_piece << ' ' << ms << '\n';
+    out << key << ' ' << t.warps_per_cta << ' ' << t.steps_per_piece << ' ' << t.prune_steps << ' ' << ms << '\n';
 }
 
 bool tune_lookup(const std::string &key, mdrl_tile *t) {
@@ -926,7 +936,7 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
         *ms = v[2];
         return MDRL_OK;
     };
-    const mdrl_tile def = {kFW, kStepsPerPiece};
+    const mdrl_tile def = {kFW, kStepsPerPiece, 0};
     mdrl_tile pick = def;
     float pick_ms = 0.0f, def_ms = 0.0f;
     const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick);
@@ -937,13 +947,16 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
         pick_ms = 3.0e38f;
         const int nfw = c->p.accum == MDRL_ACC_FIXED64 ? 2 : 1;
         for (int a = 0; a < nfw; ++a)
-            for (int spp : kTuneSpp) {
-                const mdrl_tile t = {a == 0 ? 4 : 8, spp};
-                float ms;
-                MDRL_TRY(time_tile(t, &ms));
-                if (t.warps_per_cta == def.warps_per_cta && t.steps_per_piece == def.steps_per_piece) def_ms = ms;
-                if (ms < pick_ms) { pick_ms = ms; pick = t; }
-            }
+            for (int spp : kTuneSpp)
+                for (int pr = 0; pr < nfw; ++pr) {   /* pruning exists with fixed point only */
+                    const mdrl_tile t = {a == 0 ? 4 : 8, spp, pr};
+                    float ms;
+                    MDRL_TRY(time_tile(t, &ms));
+                    if (t.warps_per_cta == def.warps_per_cta && t.steps_per_piece == def.steps_per_piece &&
+                        t.prune_steps == def.prune_steps)
+                        def_ms = ms;
+                    if (ms < pick_ms) { pick_ms = ms; pick = t; }
+                }
         tune_store(key, pick, pick_ms);
     }
     MDRL_TRY(set_tile(c, &pick, true));

@@ -323,13 +323,13 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
 static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const int *type, bool extra,
                                       unsigned long long *F64) {
     mdrl_ctx *c = b->c;
-    force_fn fn = pick_force_batch(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra);
+    force_fn fn = pick_force_batch(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->tile.prune_steps != 0);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, kBatchFT / 32);
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<b->nitems, kBatchFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
                                                   c->p.ntypes, c->ke, b->ntot, F64, nullptr, c->d_cnt, c->d_unit,
-                                                  b->d_items, b->d_reps, c->tile.steps_per_piece);
+                                                  b->d_items, b->d_reps, tile_word(c->tile.steps_per_piece, c->tile.prune_steps));
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -623,7 +623,7 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
         *ms = v[2];
         return MDRL_OK;
     };
-    const mdrl_tile def = {kBatchFT / 32, kStepsPerPiece};
+    const mdrl_tile def = {kBatchFT / 32, kStepsPerPiece, 0};
     mdrl_tile pick = def;
     float pick_ms = 0.0f, def_ms = 0.0f;
     const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick) && pick.warps_per_cta == 4;
@@ -632,13 +632,14 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
         if (default_ms) MDRL_TRY(time_tile(def, &def_ms));
     } else {
         pick_ms = 3.0e38f;
-        for (int spp : {3, 4, 6, 8, 12}) {
-            const mdrl_tile t = {kBatchFT / 32, spp};
-            float ms;
-            MDRL_TRY(time_tile(t, &ms));
-            if (spp == def.steps_per_piece) def_ms = ms;
-            if (ms < pick_ms) { pick_ms = ms; pick = t; }
-        }
+        for (int spp : {3, 4, 6, 8, 12})
+            for (int pr = 0; pr < 2; ++pr) {
+                const mdrl_tile t = {kBatchFT / 32, spp, pr};
+                float ms;
+                MDRL_TRY(time_tile(t, &ms));
+                if (spp == def.steps_per_piece && pr == def.prune_steps) def_ms = ms;
+                if (ms < pick_ms) { pick_ms = ms; pick = t; }
+            }
         tune_store(key, pick, pick_ms);
     }
     MDRL_TRY(set_tile(c, &pick, false));

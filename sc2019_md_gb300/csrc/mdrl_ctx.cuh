@@ -105,7 +105,7 @@ struct mdrl_ctx {
     bool graph_extra = false;
 
     /* force-kernel tile (mdrl_set_tile / mdrl_autotune) */
-    mdrl_tile tile = {mdrl::kFW, mdrl::kStepsPerPiece};
+    mdrl_tile tile = {mdrl::kFW, mdrl::kStepsPerPiece, 0};
 };
 
 namespace mdrl {

@@ -34,6 +34,8 @@
  */
 #pragma once
 
+#include <type_traits>
+
 #include "mdrl_kernels.cuh"
 
 namespace mdrl {
@@ -50,6 +52,9 @@ namespace mdrl {
 constexpr int kFW = MDRL_FORCE_WARPS;  /* default warps per force CTA (tiles may use 8) */
 constexpr int kFT = kFW * 32;
 constexpr int kStepsPerPiece = MDRL_STEPS_PER_PIECE;   /* default j-steps (of 8 particles) per piece */
+/* The tile word a force launch takes: steps per piece in bits 0-7 (pruning is a template
+ * parameter of the kernel; bit 8 records it). */
+inline int tile_word(int steps_per_piece, int prune) { return (steps_per_piece & 0xff) | ((prune ? 1 : 0) << 8); }
 constexpr int kFCtas = MDRL_FORCE_CTAS_PER_SM;         /* resident CTAs per SM the registers allow */
 constexpr int kBatchFT = 128;          /* threads of a batched-replica CTA (4 warps) */
 
@@ -62,10 +67,10 @@ typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDe
 /* Work items (one per unit): the result slots k_totals sums. */
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
 
-/* fw: warps per CTA (8 only with int64 fixed point; otherwise 4) */
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw = kFW);
-/* the batched-replica instantiation (int64 fixed point, per-pair wrap) */
-force_fn pick_force_batch(int order, bool sep, bool extra);
+/* fw: warps per CTA (8 only with int64 fixed point); prune: survivor lists (fixed point only) */
+force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw = kFW, bool prune = false);
+/* the batched-replica instantiation (int64 fixed point, difference rule per item) */
+force_fn pick_force_batch(int order, bool sep, bool extra, bool prune);
 
 inline size_t force_smem_bytes(int ntypes, bool extra, int fw = kFW) {
     return sizeof(float4) * (2 * kChunk + ntypes * ntypes) + sizeof(int) * 2 * kChunk +
@@ -109,10 +114,16 @@ __device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2,
     }
 }
 
-template <bool WRAP>
+/* Pair difference rules of a unit (both give the reference's d for every pair that can pass the
+ * filter; see k_force):
+ *   kDiffShift  fl(fl(xi - xj) + s)        (the unit's -L/0/+L shift, >= 4 cells per axis)
+ *   kDiffWrap   the one-wrap rule per pair (3-cell grids, cell pairs of small boxes) */
+enum : int { kDiffShift = 1, kDiffWrap = 2 };
+
+template <int MODE>
 __device__ __forceinline__ float pair_diff(float a, float b, float L, float h, float s) {
     const float d = __fsub_rn(a, b);
-    return WRAP ? wrap_d(d, L, h) : __fadd_rn(d, s);
+    return MODE == kDiffWrap ? wrap_d(d, L, h) : __fadd_rn(d, s);
 }
 
 /* Sum of v over the 8 column lanes, scattered: on return lane col holds, in v[0..2], the sums of
@@ -299,9 +310,8 @@ __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, 
 }
 
 /* One unit: home-cell particles [hs, hs + ni_all) against neighbour-cell particles
- * [cs, cs + nj_all) (the same cell when self), per-unit shift (sx, sy, sz) or, with WRAP, the
- * per-pair one-wrap rule; writes the unit's totals to uout[blockIdx.x]. */
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, int FW>
+ * [cs, cs + nj_all) (the same cell when self), with the pair-difference rule MODE (kDiff*); writes the unit's totals to uout[blockIdx.x]. */
+template <int ORDER, bool SEP, bool EXTRA, int ACC, int MODE, int FW, bool PRUNE>
 __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const int *__restrict__ ptype,
                                            int hs, int ni_all, int cs, int nj_all, bool self, const Geom &g,
                                            float sx, float sy, float sz, const TableDev &tab,
@@ -309,7 +319,9 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                                            unsigned long long *__restrict__ F64, float *__restrict__ F32,
                                            int *__restrict__ counts, UnitOut *__restrict__ uout, float4 *sIp,
                                            float4 *sJp, float4 *sCoef, int *sIt, int *sJt, float *sF, int *sC,
-                                           double (*s_red)[3], unsigned long long (*s_cnt)[2], int spp) {
+                                           double (*s_red)[3], unsigned long long (*s_cnt)[2], int tilecfg) {
+    const int spp = tilecfg & 0xff;               /* j-steps per piece */
+    constexpr bool prune = PRUNE;                 /* survivor lists (below) */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
     const bool coul = ke != 0.0f;
@@ -318,6 +330,17 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     float *wFj = wFi + 3 * kChunk;
     int *wCi = sC + warp * 2 * kChunk;
     int *wCj = wCi + kChunk;
+
+    /* Survivor lists (when the tile asks for pruning): the (32-i tile, 8-j step) pairs of a chunk
+     * whose bounding boxes come within rc.  A lower bound on every pair's r2 from the two boxes decides; the half widths carry a
+     * margin of 2^-20 x the largest box edge, above the rounding of the box centres, widths and
+     * gaps and of the pair differences, so a dropped step holds no pair that passes the filter. */
+    __shared__ float4 s_tb[2][kChunk / 32];
+    __shared__ float4 s_sb[2][kChunk / 8];
+    __shared__ unsigned s_mask[(kChunk / 32) * (kChunk / 8) / 32];
+    __shared__ int s_nsurv[kChunk / 32];
+    __shared__ unsigned char s_list[kChunk / 32][kChunk / 8];
+    const float margin = 9.5367431640625e-07f * fmaxf(g.L[0], fmaxf(g.L[1], g.L[2]));
 
     for (int t = tid; t < ntypes * ntypes; t += (FW * 32)) sCoef[t] = pcoef[t];
 
@@ -344,22 +367,92 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
 
             const int nti = (ni + 31) >> 5;
             const int S = (nj + 7) >> 3;                         /* j-steps of 8 */
-            /* pieces: tile ti covers steps [first(ti), S) in runs of spp */
-            int npieces = 0;
-            for (int ti = 0; ti < nti; ++ti) {
-                const int first = diag ? 4 * ti : 0;
-                npieces += (S - first + spp - 1) / spp;
+            if constexpr (PRUNE) {
+            /* boxes: a warp reduces each of its tiles over the 32 lanes; a thread each step */
+            for (int ti = warp; ti < nti; ti += FW) {
+                const int il = ti * 32 + lane;
+                float lx = 3.0e38f, ly = 3.0e38f, lz = 3.0e38f, ux = -3.0e38f, uy = -3.0e38f, uz = -3.0e38f;
+                if (il < ni) {
+                    const float4 pp = sIp[il];
+                    lx = ux = pp.x; ly = uy = pp.y; lz = uz = pp.z;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+                    ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+                    lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+                    ux = fmaxf(ux, __shfl_xor_sync(0xffffffffu, ux, o));
+                    uy = fmaxf(uy, __shfl_xor_sync(0xffffffffu, uy, o));
+                    uz = fmaxf(uz, __shfl_xor_sync(0xffffffffu, uz, o));
+                }
+                if (lane == 0) {
+                    /* the unit's shift folds into the centre: d = xi - xj + s */
+                    const bool sh = MODE == kDiffShift;
+                    s_tb[0][ti] = make_float4(0.5f * (lx + ux) + (sh ? sx : 0.0f), 0.5f * (ly + uy) + (sh ? sy : 0.0f),
+                                              0.5f * (lz + uz) + (sh ? sz : 0.0f), 0.0f);
+                    s_tb[1][ti] = make_float4(0.5f * (ux - lx) + margin, 0.5f * (uy - ly) + margin,
+                                              0.5f * (uz - lz) + margin, 0.0f);
+                }
             }
+            for (int st = tid; st < S; st += FW * 32) {
+                float lx = 3.0e38f, ly = 3.0e38f, lz = 3.0e38f, ux = -3.0e38f, uy = -3.0e38f, uz = -3.0e38f;
+                for (int u = 0; u < 8 && 8 * st + u < nj; ++u) {
+                    const float4 pp = sJp[8 * st + u];
+                    lx = fminf(lx, pp.x); ly = fminf(ly, pp.y); lz = fminf(lz, pp.z);
+                    ux = fmaxf(ux, pp.x); uy = fmaxf(uy, pp.y); uz = fmaxf(uz, pp.z);
+                }
+                s_sb[0][st] = make_float4(0.5f * (lx + ux), 0.5f * (ly + uy), 0.5f * (lz + uz), 0.0f);
+                s_sb[1][st] = make_float4(0.5f * (ux - lx), 0.5f * (uy - ly), 0.5f * (uz - lz), 0.0f);
+            }
+            __syncthreads();
+            /* survivor bit of pair q = ti * S + st (steps before 4 ti are the diagonal's lower half) */
+            for (int q0 = warp * 32; q0 < nti * S; q0 += FW * 32) {
+                const int q = q0 + lane;
+                bool keep = false;
+                if (q < nti * S) {
+                    const int ti = q / S, st = q - ti * S;
+                    if (!diag || st >= 4 * ti) {
+                        const float4 tc = s_tb[0][ti], th = s_tb[1][ti], jc = s_sb[0][st], jh = s_sb[1][st];
+                        float ex = tc.x - jc.x, ey = tc.y - jc.y, ez = tc.z - jc.z;
+                        if (MODE == kDiffWrap) {
+                            ex = wrap_d(ex, g.L[0], g.h[0]); ey = wrap_d(ey, g.L[1], g.h[1]); ez = wrap_d(ez, g.L[2], g.h[2]);
+                        }
+                        const float gx = fmaxf(fabsf(ex) - (th.x + jh.x), 0.0f);
+                        const float gy = fmaxf(fabsf(ey) - (th.y + jh.y), 0.0f);
+                        const float gz = fmaxf(fabsf(ez) - (th.z + jh.z), 0.0f);
+                        keep = gx * gx + gy * gy + gz * gz <= g.rc2;
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, keep);
+                if (lane == 0) s_mask[q0 >> 5] = b;
+            }
+            __syncthreads();
+            for (int ti = tid; ti < nti; ti += FW * 32) {
+                int c = 0;
+                for (int st = 0; st < S; ++st) {
+                    const int q = ti * S + st;
+                    if ((s_mask[q >> 5] >> (q & 31)) & 1u) s_list[ti][c++] = (unsigned char)st;
+                }
+                s_nsurv[ti] = c;
+            }
+            __syncthreads();
+            }
+            /* pieces: runs of spp steps of one tile -- its surviving steps, or without pruning the
+             * steps [first, S) with first = 4 ti on the diagonal */
+            int npieces = 0;
+            for (int ti = 0; ti < nti; ++ti)
+                npieces += ((prune ? s_nsurv[ti] : S - (diag ? 4 * ti : 0)) + spp - 1) / spp;
             for (int p = warp; p < npieces; p += FW) {
-                int ti = 0, r = p, first = 0, cnt = 0;
+                int ti = 0, r = p, nst = 0;
                 for (;; ++ti) {
-                    first = diag ? 4 * ti : 0;
-                    cnt = (S - first + spp - 1) / spp;
+                    nst = prune ? s_nsurv[ti] : S - (diag ? 4 * ti : 0);
+                    const int cnt = (nst + spp - 1) / spp;
                     if (r < cnt) break;
                     r -= cnt;
                 }
-                const int s0 = first + r * spp;
-                const int s1 = min(S, s0 + spp);
+                const int base = prune ? 0 : (diag ? 4 * ti : 0);
+                const int k0 = r * spp;
+                const int k1 = min(nst, k0 + spp);
                 float xi[8], yi[8], zi[8], qi[8];
                 int tti[8];
 #pragma unroll
@@ -378,8 +471,8 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
 #pragma unroll
                 for (int t = 0; t < 24; ++t) fi[t] = 0.0f;
                 int ci[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                for (int s = s0; s < s1; ++s) {
-                    const int jl = s * 8 + col;
+                for (int kk = k0; kk < k1; ++kk) {
+                    const int jl = (prune ? (int)s_list[ti][kk] : base + kk) * 8 + col;
                     float xj = -far, yj = -far, zj = -far, qj = 0.0f;
                     int ttj = 0;
                     if (jl < nj) {
@@ -396,9 +489,9 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     unsigned okm = 0;
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
-                        const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
-                        const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                        const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
+                        const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
+                        const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
                         r2k[k] = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                         bool ok = (r2k[k] > 0.0f) && (r2k[k] <= g.rc2);
                         if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
@@ -407,16 +500,16 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         if (okm & (1u << k)) {
-                            const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
-                            const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
-                            const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                            const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
+                            const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
+                            const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
                             const float r2 = r2k[k];
 #else
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
-                        const float dx = pair_diff<WRAP>(xi[k], xj, g.L[0], g.h[0], sx);
-                        const float dy = pair_diff<WRAP>(yi[k], yj, g.L[1], g.h[1], sy);
-                        const float dz = pair_diff<WRAP>(zi[k], zj, g.L[2], g.h[2], sz);
+                        const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
+                        const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
+                        const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
                         const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
                                                    __fmul_rn(dz, dz));
                         bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
@@ -528,13 +621,13 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     }
 }
 
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false, int FW = kFW>
+template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false, int FW = kFW, bool PRUNE = false>
 __global__ void __launch_bounds__(FW * 32, (FW == kFW ? kFCtas : 16 / FW))
 k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         const int *__restrict__ cstart, Geom gparam, TableDev tab, const float4 *__restrict__ pcoef,
         int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
         float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout,
-        const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int spp) {
+        const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int tilecfg) {
     extern __shared__ float4 smem[];
     float4 *sIp = smem;
     float4 *sJp = sIp + kChunk;
@@ -624,20 +717,70 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     }
     const int hs = cstart[coff + h], ni_all = cstart[coff + h + 1] - hs;
     const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
-    if constexpr (BATCH) {
-        if (use_wrap)
-            force_unit<ORDER, SEP, EXTRA, ACC, true, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
-                                                     pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
-                                                     sCoef, sIt, sJt, sF, sC, s_red, s_cnt, spp);
-        else
-            force_unit<ORDER, SEP, EXTRA, ACC, false, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
-                                                      pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp,
-                                                      sCoef, sIt, sJt, sF, sC, s_red, s_cnt, spp);
-    } else {
-        force_unit<ORDER, SEP, EXTRA, ACC, WRAP, FW>(pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab,
-                                                 pcoef, ntypes, ke, n, F64, F32, counts, uout, sIp, sJp, sCoef,
-                                                 sIt, sJt, sF, sC, s_red, s_cnt, spp);
+#define MDRL_UNIT_ARGS pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab, pcoef, ntypes, ke, n, F64, F32, \
+                       counts, uout, sIp, sJp, sCoef, sIt, sJt, sF, sC, s_red, s_cnt, tilecfg
+    /* one unit body per kernel where the rule is fixed (a second body cost more in instruction
+     * fetch than a skipped add saves); the batch picks per item */
+    if (use_wrap)
+        force_unit<ORDER, SEP, EXTRA, ACC, kDiffWrap, FW, PRUNE>(MDRL_UNIT_ARGS);
+    else
+        force_unit<ORDER, SEP, EXTRA, ACC, kDiffShift, FW, PRUNE>(MDRL_UNIT_ARGS);
+#undef MDRL_UNIT_ARGS
+}
+
+/* ---- instantiation sets ----------------------------------------------------------------------
+ * Each set is instantiated explicitly in one translation unit (mdrl_force_*.cu), so the sets
+ * compile in parallel; everywhere else the declarations below keep them from being instantiated. */
+template <int ACC, int FW, bool PRUNE>
+force_fn pick_force_set(int order, bool sep, bool extra, bool wrap) {
+    auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
+        constexpr int O = decltype(ord)::value;
+        constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
+        return wrap ? (force_fn)k_force<O, S, E, ACC, true, false, FW, PRUNE>
+                    : (force_fn)k_force<O, S, E, ACC, false, false, FW, PRUNE>;
+    };
+    auto se = [&](auto ord) -> force_fn {
+        using T = std::true_type;
+        using F = std::false_type;
+        if (sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});
+        return extra ? w(ord, F{}, T{}) : w(ord, F{}, F{});
+    };
+    switch (order) {
+        case 0: return se(std::integral_constant<int, 0>{});
+        case 1: return se(std::integral_constant<int, 1>{});
+        case 2: return se(std::integral_constant<int, 2>{});
+        default: return se(std::integral_constant<int, 3>{});
     }
 }
+
+template <bool PRUNE>
+force_fn pick_batch_set(int order, bool sep, bool extra) {
+    auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
+        constexpr int O = decltype(ord)::value;
+        constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
+        return (force_fn)k_force<O, S, E, 0, true, true, kBatchFT / 32, PRUNE>;
+    };
+    auto se = [&](auto ord) -> force_fn {
+        using T = std::true_type;
+        using F = std::false_type;
+        if (sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});
+        return extra ? w(ord, F{}, T{}) : w(ord, F{}, F{});
+    };
+    switch (order) {
+        case 0: return se(std::integral_constant<int, 0>{});
+        case 1: return se(std::integral_constant<int, 1>{});
+        case 2: return se(std::integral_constant<int, 2>{});
+        default: return se(std::integral_constant<int, 3>{});
+    }
+}
+
+extern template force_fn pick_force_set<0, 4, false>(int, bool, bool, bool);
+extern template force_fn pick_force_set<0, 4, true>(int, bool, bool, bool);
+extern template force_fn pick_force_set<0, 8, false>(int, bool, bool, bool);
+extern template force_fn pick_force_set<0, 8, true>(int, bool, bool, bool);
+extern template force_fn pick_force_set<1, 4, false>(int, bool, bool, bool);
+extern template force_fn pick_force_set<2, 4, false>(int, bool, bool, bool);
+extern template force_fn pick_batch_set<false>(int, bool, bool);
+extern template force_fn pick_batch_set<true>(int, bool, bool);
 
 }  // namespace mdrl

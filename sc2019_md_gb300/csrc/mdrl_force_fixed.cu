@@ -1,40 +1,11 @@
 /*
- * mdrl_force_fixed.cu — instantiations of the half-shell force kernel with
- * int64 fixed-point accumulation (one translation unit per accumulation mode so
- * that they compile in parallel).
+ * mdrl_force_fixed.cu — the force-kernel instantiations for int64 fixed-point accumulation, 4 warps per CTA: one
+ * instantiation set per translation unit so that the sets compile in parallel.
  */
 #include "mdrl_force.cuh"
 
 namespace mdrl {
 
-template <int ORDER, bool SEP, bool EXTRA, int FW>
-static force_fn pick_wrap_0(bool wrap) {
-    return wrap ? (force_fn)k_force<ORDER, SEP, EXTRA, 0, true, false, FW>
-                : (force_fn)k_force<ORDER, SEP, EXTRA, 0, false, false, FW>;
-}
-
-template <int ORDER, int FW>
-static force_fn pick_order_0(bool sep, bool extra, bool wrap) {
-    if (sep) return extra ? pick_wrap_0<ORDER, true, true, FW>(wrap) : pick_wrap_0<ORDER, true, false, FW>(wrap);
-    return extra ? pick_wrap_0<ORDER, false, true, FW>(wrap) : pick_wrap_0<ORDER, false, false, FW>(wrap);
-}
-
-template <int FW>
-static force_fn pick_fw_0(int order, bool sep, bool extra, bool wrap) {
-    switch (order) {
-        case 0: return pick_order_0<0, FW>(sep, extra, wrap);
-        case 1: return pick_order_0<1, FW>(sep, extra, wrap);
-        case 2: return pick_order_0<2, FW>(sep, extra, wrap);
-        default: return pick_order_0<3, FW>(sep, extra, wrap);
-    }
-}
-
-/* The 8-warp instantiations compile in their own translation unit (mdrl_force_fixed8.cu). */
-force_fn pick_force_acc0_w8(int order, bool sep, bool extra, bool wrap);
-
-/* Fixed point is the tuned mode: CTAs of 4 or 8 warps. */
-force_fn pick_force_acc0(int order, bool sep, bool extra, bool wrap, int fw) {
-    return fw == 8 ? pick_force_acc0_w8(order, sep, extra, wrap) : pick_fw_0<4>(order, sep, extra, wrap);
-}
+template force_fn pick_force_set<0, 4, false>(int, bool, bool, bool);
 
 }  // namespace mdrl

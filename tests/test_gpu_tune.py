@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 SUM_TOL = 2e-6
 FIX_ABS = 64 * 2.0 ** -24
-CANDIDATES = {(w, s) for w in (4, 8) for s in (3, 4, 6, 8, 12)}
+CANDIDATES = {(w, s, p) for w in (4, 8) for s in (3, 4, 6, 8, 12) for p in (0, 1)}
 
 
 @pytest.fixture(scope="module")
@@ -31,8 +31,12 @@ def sysm():
     return systems.small_ljc(3000, 37.5, 12.0, seed=21)     # 3 x 3 x 3 cells, ~110 per cell
 
 
-@pytest.mark.parametrize("tile", [(4, 3), (4, 12), (8, 6), (8, 1), (4, 32)])
-def test_tile_parity_and_reproducibility(sysm, tile):
+@pytest.mark.parametrize("tile", [(4, 3, 0), (4, 12, 1), (8, 6, 1), (8, 1, 0), (4, 32, 1), (4, 6, 1)])
+@pytest.mark.parametrize("grid", ["3 cells (per-pair wrap)", "4 cells (per-unit shift)"])
+def test_tile_parity_and_reproducibility(sysm, tile, grid):
+    if grid.startswith("4"):
+        sysm = systems.small_ljc(6400, 50.0, 12.0, seed=22)
+        assert sysm.ncell == (4, 4, 4)
     p = sysm.params(table_bins=512, flags=m.FLAG_ENERGY)
     x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
     with m.Context(p) as ctx:
@@ -98,8 +102,8 @@ def test_tune_cache_file_across_processes(tmp_path):
         outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
     lines = cache.read_text().strip().splitlines()
     assert len(lines) == 1                         # the second process read it instead of tuning
-    key, w, s, ms = lines[0].split()
-    assert (int(w), int(s)) == tuple(outs[0]["tile"]) == tuple(outs[1]["tile"])
+    key, w, s, pr, ms = lines[0].split()
+    assert (int(w), int(s), int(pr)) == tuple(outs[0]["tile"]) == tuple(outs[1]["tile"])
 
 
 def test_batch_autotune_and_tile_parity():
@@ -109,17 +113,17 @@ def test_batch_autotune_and_tile_parity():
     with m.Batch(p, spec) as b:
         b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
         r = b.autotune(retime=True)
-        assert r["tile"][0] == 4 and r["tile"][1] in (3, 4, 6, 8, 12)
+        assert r["tile"][0] == 4 and r["tile"][1] in (3, 4, 6, 8, 12) and r["tile"][2] in (0, 1)
         assert 0 < r["ms"] <= r["default_ms"]
         with pytest.raises(m.MdrlError):
             b.set_tile(8, 6)
-        b.set_tile(4, 3)
+        b.set_tile(4, 3, 1)
         F, _, _ = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t)
         offs = b.offsets
     for k in (1, 2):                               # half-shell replicas: equal to a lone context
         s = reps[k]
         with m.Context(s.params(table_bins=512)) as ctx:
-            ctx.set_tile(4, 3)
+            ctx.set_tile(4, 3, 1)
             F1, _, _ = ctx.force(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.q, s.type)
         assert np.array_equal(F[offs[k]:offs[k + 1]].view(np.uint32), F1.view(np.uint32))
 
@@ -133,5 +137,9 @@ def test_tile_validation(sysm):
             ctx.set_tile(4, 0)
         with pytest.raises(m.MdrlError):
             ctx.set_tile(2, 6)
+        with pytest.raises(m.MdrlError):
+            ctx.set_tile(4, 6, 2)
+        with pytest.raises(m.MdrlError):
+            ctx.set_tile(4, 6, 1)                   # pruned kernels exist for fixed point only
         ctx.set_tile(4, 12)
-        assert ctx.tile() == (4, 12)
+        assert ctx.tile() == (4, 12, 0)
