@@ -271,6 +271,29 @@ mdrl_status mdrl_batch_time_force(mdrl_batch *batch, float *ms);
 /* See mdrl_set_pair_coefficients. */
 mdrl_status mdrl_batch_set_pair_coefficients(mdrl_batch *batch, const double *coef);
 
+/* ---- long-range electrostatics (smooth particle-mesh Ewald) -------------------------------
+ * No counterpart on the reference's RL path, which truncates Coulomb at rc (its Long_Range/ RTL
+ * is a partial PME: B-spline coefficients on a 4x4x4 patch, a 16^3 grid, FFT cores).  With PME
+ * on, the Coulomb table slots hold the Ewald real-space pair erfc(beta r)/r (the tables are
+ * refitted), and every force evaluation, step and energy adds the reciprocal-space part
+ * (B-spline charge spreading into an int64 fixed-point grid, 3-D FFTs, the influence function,
+ * force gather into the same accumulators) plus the self and neutralising-background energies.
+ * e_coul then holds the full Ewald energy; the virial covers the real-space pairs only.
+ * Single-system contexts only. */
+typedef struct {
+    double beta;        /* Ewald splitting (1/A); 0: the beta with erfc(beta rc) = tolerance */
+    double tolerance;   /* default 1e-5 */
+    double spacing;     /* target grid spacing (A) for axes whose grid is 0; default 1.0 */
+    int grid[3];        /* FFT points per axis; 0: from spacing, rounded up to 2^a 3^b 5^c 7^d */
+    int order;          /* B-spline order, 4 or 6; default 4 */
+} mdrl_pme_params;
+
+void mdrl_default_pme_params(mdrl_pme_params *p);
+/* p = NULL switches PME off (and refits the plain Coulomb tables). */
+mdrl_status mdrl_set_pme(mdrl_ctx *ctx, const mdrl_pme_params *p);
+/* The resolved parameters (beta, grid) and whether PME is on. */
+mdrl_status mdrl_get_pme(mdrl_ctx *ctx, mdrl_pme_params *p, int *enabled);
+
 /* ---- tiles and the autotuner ---------------------------------------------------------------
  * No counterpart in the reference.  mdrl_autotune times the force kernel (mdrl_time_force's
  * launch, median of 5) for every candidate tile on the context's current state (call it after

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
         L.orc_force_allpairs_mt.restype = C.c_int64
         L.orc_force_allimage.argtypes = [C.POINTER(OrcSys), _D, _D, _D, _I, C.POINTER(OrcStats)]
         L.orc_force_allimage.restype = C.c_int64
+        L.orc_ewald64.argtypes = [C.POINTER(OrcSys), C.c_double, C.c_int, _D, _D]
         L.orc_cmodel_run.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, _F, _F, _F, _I]
         _lib = L
     return _lib
@@ -137,6 +138,14 @@ class System:
                                      C.byref(st))
         assert r >= 0
         return F, F32, A, cnt, st.as_dict()
+
+    def ewald64(self, beta, nmax, forces=True):
+        """FP64 Ewald sum (see oracle.h): (F (n,3) or None, {'real', 'recip', 'self', 'background',
+        'total'})."""
+        F = np.zeros((self.n, 3)) if forces else None
+        e = np.zeros(4)
+        assert lib().orc_ewald64(C.byref(self.s), float(beta), int(nmax), _p(F, _D), _p(e, _D)) == 0
+        return F, {"real": e[0], "recip": e[1], "self": e[2], "background": e[3], "total": float(e.sum())}
 
     def pair(self, xi, xj, qi=0.0, qj=0.0, ti=0, tj=0):
         out = np.zeros(8, np.float32)

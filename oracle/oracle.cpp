@@ -8,6 +8,8 @@
 #include "oracle.h"
 
 #include <math.h>
+
+#include <cmath>
 #include <stdlib.h>
 #include <string.h>
 
@@ -520,6 +522,96 @@ int64_t orc_force_allimage(const orc_sys *s, double *F, double *F32sum, double *
         }
     if (st) *st = acc;
     return acc.pairs;
+}
+
+int orc_ewald64(const orc_sys *s, double beta, int nmax, double *F, double *energy) {
+    if (!s || s->n < 0 || !s->q || beta <= 0.0 || nmax < 1) return -1;
+    const int n = s->n;
+    const double ke = s->ke64;
+    const double L[3] = {s->box[0], s->box[1], s->box[2]};
+    const double V = L[0] * L[1] * L[2];
+    const double rc2 = s->rc2;
+    const double PI = 3.14159265358979323846;
+    if (F) memset(F, 0, sizeof(double) * 3 * n);
+    double e_real = 0.0, e_rec = 0.0, qsum = 0.0, q2sum = 0.0;
+    std::vector<double> P(3 * (size_t)n), Q(n);
+    for (int i = 0; i < n; ++i) {
+        P[3 * i] = s->x[i]; P[3 * i + 1] = s->y[i]; P[3 * i + 2] = s->z[i];
+        Q[i] = s->q[i];
+        qsum += Q[i];
+        q2sum += Q[i] * Q[i];
+    }
+    /* real space */
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            double d[3], r2 = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                d[a] = P[3 * i + a] - P[3 * j + a];
+                d[a] -= L[a] * std::floor(d[a] / L[a] + 0.5);
+                r2 += d[a] * d[a];
+            }
+            if (!(r2 > 0.0 && r2 <= rc2)) continue;
+            const double r = std::sqrt(r2);
+            const double qq = ke * Q[i] * Q[j];
+            e_real += qq * std::erfc(beta * r) / r;
+            if (F) {
+                const double fs = qq * (std::erfc(beta * r) / r + 2.0 * beta / std::sqrt(PI) * std::exp(-beta * beta * r2)) / r2;
+                for (int a = 0; a < 3; ++a) { F[3 * i + a] += fs * d[a]; F[3 * j + a] -= fs * d[a]; }
+            }
+        }
+    /* reciprocal space over the half space of n (n and -n contribute alike) */
+    const int w = 2 * nmax + 1;
+    std::vector<double> cr[3], ci[3];   /* cos / sin(2 pi k x_j / L) for k = -nmax..nmax */
+    for (int a = 0; a < 3; ++a) {
+        cr[a].resize((size_t)n * w);
+        ci[a].resize((size_t)n * w);
+        for (int j = 0; j < n; ++j)
+            for (int k = -nmax; k <= nmax; ++k) {
+                const double t = 2.0 * PI * k * P[3 * j + a] / L[a];
+                cr[a][(size_t)j * w + k + nmax] = std::cos(t);
+                ci[a][(size_t)j * w + k + nmax] = std::sin(t);
+            }
+    }
+    std::vector<double> er(n), ei(n);
+    for (int n1 = 0; n1 <= nmax; ++n1)
+        for (int n2 = -nmax; n2 <= nmax; ++n2)
+            for (int n3 = -nmax; n3 <= nmax; ++n3) {
+                if (n1 == 0 && (n2 < 0 || (n2 == 0 && n3 <= 0))) continue;   /* half space, no m = 0 */
+                const double m[3] = {n1 / L[0], n2 / L[1], n3 / L[2]};
+                const double m2 = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+                const double g = std::exp(-PI * PI * m2 / (beta * beta)) / m2;
+                if (g < 1e-300) continue;
+                double sr = 0.0, si = 0.0;
+                for (int j = 0; j < n; ++j) {
+                    const size_t o = (size_t)j * w;
+                    /* e = e1 e2 e3 */
+                    const double ar = cr[0][o + n1 + nmax], ai = ci[0][o + n1 + nmax];
+                    const double br = cr[1][o + n2 + nmax], bi = ci[1][o + n2 + nmax];
+                    const double cr3 = cr[2][o + n3 + nmax], ci3 = ci[2][o + n3 + nmax];
+                    const double abr = ar * br - ai * bi, abi = ar * bi + ai * br;
+                    er[j] = abr * cr3 - abi * ci3;
+                    ei[j] = abr * ci3 + abi * cr3;
+                    sr += Q[j] * er[j];
+                    si += Q[j] * ei[j];
+                }
+                e_rec += 2.0 * g * (sr * sr + si * si);
+                if (F) {
+                    /* F_j = (2 ke q_j / V) sum_m g m Im[conj(S) e_j], both half spaces */
+                    const double c = 2.0 * 2.0 * ke / V * g;
+                    for (int j = 0; j < n; ++j) {
+                        const double im = sr * ei[j] - si * er[j];
+                        for (int a = 0; a < 3; ++a) F[3 * j + a] += c * Q[j] * m[a] * im;
+                    }
+                }
+            }
+    e_rec *= ke / (2.0 * PI * V);
+    if (energy) {
+        energy[0] = e_real;
+        energy[1] = e_rec;
+        energy[2] = -ke * beta / std::sqrt(PI) * q2sum;
+        energy[3] = -ke * PI * qsum * qsum / (2.0 * V * beta * beta);
+    }
+    return 0;
 }
 
 /* SC/C_Model_ForceEval/MD_Evaluation_Model.cpp, restated.  Line numbers refer to that file.

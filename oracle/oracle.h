@@ -20,6 +20,10 @@
  *                      (rc, 3 rc) where the half shell does not apply (no counterpart in the
  *                      reference, which requires 3 cells per axis; the pair datapath is
  *                      orc_pair_f32's, the forces the FP64 table evaluation of orc_force_tables64)
+ *   orc_ewald64        FP64 Ewald sum of the point charges (real space erfc within rc, reciprocal
+ *                      space as a direct sum over wave vectors, self and background terms): the
+ *                      checker of the long-range (PME) path; no counterpart in the reference, whose
+ *                      RL path truncates Coulomb at rc (its Long_Range/ RTL is a partial PME)
  *   orc_cmodel_run     SC/C_Model_ForceEval/MD_Evaluation_Model.cpp:57-203, expression by expression
  *
  * Parity is pinned by the reference's own fixtures (tests/golden/, see make_golden.py) and by
@@ -102,6 +106,17 @@ int64_t orc_force_allpairs_mt(const orc_sys *s, int nthreads, float *F);
  * unordered pairs, -1 on error. */
 int64_t orc_force_allimage(const orc_sys *s, double *F, double *F32sum, double *Fabs, int *counts,
                            orc_stats *st);
+
+/* Ewald sum in FP64 of the charges s->q at s->x/y/z in the periodic box s->box (tin-foil
+ * boundary), prefactor ke = s->ke64:
+ *   real       ke sum_{i<j, |r_ij| <= rc} qi qj erfc(beta r)/r   (minimum image; rc^2 = s->rc2 <= (L/2)^2)
+ *   reciprocal ke / (2 pi V) sum_{m != 0, |n_a| <= nmax} exp(-pi^2 m^2 / beta^2) / m^2 |S(m)|^2,
+ *              m = (n1/L1, n2/L2, n3/L3), S(m) = sum_j q_j exp(2 pi i m . r_j)
+ *   self       -ke beta / sqrt(pi) sum q^2
+ *   background -ke pi Q^2 / (2 V beta^2)   (Q = sum q; zero for a neutral system)
+ * F (n*3, optional) receives the forces of the real and reciprocal parts; energy[4] the four terms.
+ * Returns 0, or -1 on bad input. */
+int orc_ewald64(const orc_sys *s, double beta, int nmax, double *F, double *energy);
 
 /* The reference C model, restated: n particles (positions pos[3n], velocities vel[3n], both
  * updated in place), iters iterations, box edge and cutoff as given (the reference uses 24 and

@@ -15,7 +15,7 @@ import numpy as np
 
 __all__ = [
     "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables",
-    "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
+    "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PmeParams", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
     "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
     "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "MAX_TYPES", "STATUS",
@@ -75,6 +75,15 @@ _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int)
 _D = C.POINTER(C.c_double)
 _lib = None
+
+
+class PmeParams(C.Structure):
+    _fields_ = [("beta", C.c_double), ("tolerance", C.c_double), ("spacing", C.c_double),
+                ("grid", C.c_int * 3), ("order", C.c_int)]
+
+    def as_dict(self):
+        return {"beta": self.beta, "tolerance": self.tolerance, "spacing": self.spacing,
+                "grid": tuple(self.grid), "order": self.order}
 
 
 class Tile(C.Structure):
@@ -137,6 +146,10 @@ def lib() -> C.CDLL:
     L.mdrl_batch_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
     L.mdrl_batch_replica_stats.argtypes = [vp, C.POINTER(Stats)]
     L.mdrl_batch_time_force.argtypes = [vp, _F]
+    L.mdrl_default_pme_params.argtypes = [C.POINTER(PmeParams)]
+    L.mdrl_default_pme_params.restype = None
+    L.mdrl_set_pme.argtypes = [vp, C.POINTER(PmeParams)]
+    L.mdrl_get_pme.argtypes = [vp, C.POINTER(PmeParams), _I]
     L.mdrl_set_pair_coefficients.argtypes = [vp, _D]
     L.mdrl_batch_set_pair_coefficients.argtypes = [vp, _D]
     L.mdrl_set_tile.argtypes = [vp, C.POINTER(Tile)]
@@ -144,7 +157,7 @@ def lib() -> C.CDLL:
     L.mdrl_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
     L.mdrl_batch_set_tile.argtypes = [vp, C.POINTER(Tile)]
     L.mdrl_batch_autotune.argtypes = [vp, st, C.POINTER(Tile), _F, _F]
-    for name in ("mdrl_set_pair_coefficients", "mdrl_batch_set_pair_coefficients", "mdrl_set_tile", "mdrl_get_tile", "mdrl_autotune", "mdrl_batch_set_tile", "mdrl_batch_autotune",
+    for name in ("mdrl_set_pme", "mdrl_get_pme", "mdrl_set_pair_coefficients", "mdrl_batch_set_pair_coefficients", "mdrl_set_tile", "mdrl_get_tile", "mdrl_autotune", "mdrl_batch_set_tile", "mdrl_batch_autotune",
                  "mdrl_batch_create", "mdrl_batch_destroy", "mdrl_batch_layout", "mdrl_batch_force_eval",
                  "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
                  "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
@@ -249,6 +262,28 @@ class Context:
         coef = np.ascontiguousarray(coef, dtype=np.float32)
         nfunc = coef.shape[0]
         _check(lib().mdrl_set_tables(self._h, order, nseg, bins, min_log2, nfunc, _fp(coef), int(raw)))
+
+    def set_pme(self, enable: bool = True, **kw) -> dict:
+        """Switch smooth-PME long-range electrostatics on (keywords: beta, tolerance, spacing,
+        grid, order) or off; returns the resolved parameters (or {} when off)."""
+        if not enable:
+            _check(lib().mdrl_set_pme(self._h, None))
+            return {}
+        p = PmeParams()
+        lib().mdrl_default_pme_params(C.byref(p))
+        for k, v in kw.items():
+            if k == "grid":
+                for d in range(3):
+                    p.grid[d] = int(v[d])
+            else:
+                setattr(p, k, v)
+        _check(lib().mdrl_set_pme(self._h, C.byref(p)))
+        return self.pme()
+
+    def pme(self) -> dict:
+        p, on = PmeParams(), C.c_int()
+        _check(lib().mdrl_get_pme(self._h, C.byref(p), C.byref(on)))
+        return p.as_dict() if on.value else {}
 
     def set_pair_coefficients(self, coef) -> None:
         """Per-type-pair multipliers (ntypes*ntypes, 4): A14, B8, A12, B6 (FP64)."""

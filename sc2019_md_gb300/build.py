@@ -1,5 +1,6 @@
 """Build libmdrl.so in-tree: nvcc for sm_103a (one -gencode), translation units compiled in
-parallel, cudart linked statically so the library needs no CUDA runtime on the library path."""
+parallel, cudart linked statically; cuFFT (the PME transforms) linked dynamically with an rpath to
+the toolkit that built the library."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -73,7 +74,9 @@ def build(force: bool = False, ptxas_verbose: bool = False, out_dir: Path | None
         results = list(ex.map(lambda s: _compile(s, ptxas_verbose, out, defines), srcs))
     objs = [str(o) for o, _ in results]
     tmp = out / "libmdrl.so.tmp"
-    cmd = [nvcc_path(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", str(tmp), *objs]
+    cuda_lib = Path(nvcc_path()).resolve().parent.parent / "lib64"
+    cmd = [nvcc_path(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", str(tmp), *objs, "-lcufft",
+           "-Xlinker", "-rpath", "-Xlinker", str(cuda_lib)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")

@@ -152,7 +152,7 @@ static mdrl_status check_cells(mdrl_ctx *c) {
     return MDRL_OK;
 }
 
-static mdrl_status upload_tables(mdrl_ctx *c) {
+mdrl_status mdrl::upload_tables(mdrl_ctx *c) {
     const int nidx = c->nseg * c->bins;
     const int nc = c->order + 1;
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr);
@@ -285,6 +285,7 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
         if (c->graph_exec[k]) cudaGraphExecDestroy(c->graph_exec[k]);
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
+    pme_free(c);
     free_particles(c);
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
@@ -464,8 +465,11 @@ static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const floa
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
     MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0, true));
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
+    const bool energy = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
+    MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, energy));
     k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
+    if (energy) MDRL_TRY(pme_add_energy(c, n));
     if (n > 0)
         k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, c->d_F32, c->d_cnt, fx, fy,
                                                       fz, counts);
@@ -702,10 +706,12 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
                                                       c->d_ovz, c->d_vel[0]);
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
+    MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, extra));
     k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->mt_half, 0,
                                                 c->d_kepart);
     k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
+    if (extra) MDRL_TRY(pme_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_TRY(check_device_errors(c));
@@ -733,12 +739,14 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
                                                         c->d_id[b], c->d_F64, c->d_F32);
     if (extra) MDRL_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * (size_t)n, c->stream));
     MDRL_TRY(launch_force(c, n, c->d_pos[b], c->d_type[b], extra));
+    MDRL_TRY(pme_enqueue(c, n, c->d_pos[b], c->d_F64, c->d_F32, extra));
     /* kinetic energy only when energies are requested */
     if (vv || extra)
         k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->mt_half,
                                                     vv ? 1 : 0, extra ? c->d_kepart : nullptr);
     k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
                                        c->d_kepart, c->d_tot, extra ? 1 : 0);
+    if (extra) MDRL_TRY(pme_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
 }
@@ -964,4 +972,26 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
     if (best_ms) *best_ms = pick_ms;
     if (default_ms) *default_ms = def_ms;
     return MDRL_OK;
+}
+
+/* ---- long-range electrostatics ------------------------------------------------------------- */
+
+extern "C" mdrl_status mdrl_set_pme(mdrl_ctx *c, const mdrl_pme_params *p) {
+    if (!c) { set_error("mdrl_set_pme: null context"); return MDRL_ERR_INVALID_ARG; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    if (c->stream) MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    drop_graphs(c);
+    double beta = 0.0;
+    if (p) {
+        MDRL_TRY(pme_setup(c, p));
+        mdrl_pme_params r;
+        mdrl_get_pme(c, &r, nullptr);
+        beta = r.beta;
+    } else {
+        pme_free(c);
+    }
+    /* the Coulomb slots: Ewald real-space pair with PME, plain r^-3 / r^-1 without */
+    c->raw = false;
+    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab, beta);
+    return upload_tables(c);
 }

@@ -14,6 +14,10 @@
 
 using mdrl::set_error;
 
+namespace mdrl {
+struct PmeState;
+}
+
 #define MDRL_CUDA(call)                                                                   \
     do {                                                                                  \
         cudaError_t e_ = (call);                                                          \
@@ -104,6 +108,9 @@ struct mdrl_ctx {
     int graph_n = -1;
     bool graph_extra = false;
 
+    /* long-range electrostatics (mdrl_set_pme), null when off */
+    mdrl::PmeState *pme = nullptr;
+
     /* force-kernel tile (mdrl_set_tile / mdrl_autotune) */
     mdrl_tile tile = {mdrl::kFW, mdrl::kStepsPerPiece, 0};
 };
@@ -116,6 +123,12 @@ mdrl_status check_device_errors(mdrl_ctx *c);
 /* Raise the dynamic shared-memory limit of a force kernel once per kernel and device. */
 mdrl_status prepare_force_kernel(force_fn fn, int device);
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
+/* PME (mdrl_pme.cu): setup, teardown, the reciprocal part of a force evaluation, its energies. */
+mdrl_status pme_setup(mdrl_ctx *c, const mdrl_pme_params *p);
+void pme_free(mdrl_ctx *c);
+mdrl_status pme_enqueue(mdrl_ctx *c, int n, const float4 *pos, unsigned long long *F64, float *F32, bool energy);
+mdrl_status pme_add_energy(mdrl_ctx *c, int n);
+mdrl_status upload_tables(mdrl_ctx *c);
 /* Tiles: change (re-capturing graphs), and the autotuner's process-wide cache. */
 mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8);
 bool tune_lookup(const std::string &key, mdrl_tile *t);

@@ -50,7 +50,9 @@ struct DevTotals {
     int pad;
 };
 
-void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out);
+/* beta > 0: the Coulomb slots hold the Ewald real-space pair (erfc-screened) instead of r^-3, r^-1 */
+void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out,
+                double beta = 0.0);
 void mix_pair_coefficients(const mdrl_params &p, std::vector<float> *pc, std::vector<double> *pc64);
 
 void set_error(const std::string &msg);

@@ -13,7 +13,8 @@
  *
  * The functions are unit-prefactor powers of r2 (x = r2):
  *   r^-14 = x^-7, r^-8 = x^-4, r^-3 = x^-1.5, r^-12 = x^-6, r^-6 = x^-3, r^-1 = x^-0.5,
- * and the per-pair prefactors (A14 = 48*eps*sig^12, B8 = -24*eps*sig^6, A12 = 4*eps*sig^12,
+ * or, with Ewald splitting for the long-range solver, the real-space Coulomb pair in the r^-3 and
+ * r^-1 slots, and the per-pair prefactors (A14 = 48*eps*sig^12, B8 = -24*eps*sig^6, A12 = 4*eps*sig^12,
  * B6 = -4*eps*sig^6, QQ = ke*qi*qj) multiply the table values in the kernel, as the reference's
  * LJ+Coulomb pipeline does with its p_a, p_b, p_qq ports
  * (SC/RL_Evaluate_Pairs_1st_Order.v:53-55,361-395).
@@ -66,7 +67,20 @@ static void lsq_fit(int m, int order, const double *t, const double *y, double *
     }
 }
 
-void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out) {
+/* Unit function f of the table set at x = r2: powers of x, or with Ewald splitting (beta > 0) the
+ * real-space Coulomb pair (r^-3 -> (erfc(beta r)/r + 2 beta/sqrt(pi) exp(-beta^2 r^2)) / r^2, the
+ * force over r; r^-1 -> erfc(beta r)/r, the energy). */
+static double unit_function(int f, double x, double beta) {
+    if (beta > 0.0 && (f == kF3 || f == kF1)) {
+        const double r = std::sqrt(x);
+        const double e = std::erfc(beta * r) / r;
+        if (f == kF1) return e;
+        return (e + 2.0 * beta / std::sqrt(3.14159265358979323846) * std::exp(-beta * beta * x)) / x;
+    }
+    return std::pow(x, kExponent[f]);
+}
+
+void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out, double beta) {
     const int nidx = nseg * bins;
     const int nc = order + 1;
     out->assign((size_t)kNumFunc * nc * nidx, 0.0f);
@@ -79,7 +93,7 @@ void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::v
                 const double x0 = seg_lo + j * width;
                 for (int i = 0; i < samples; ++i) {
                     t[i] = (double)i / samples;
-                    y[i] = std::pow(x0 + t[i] * width, kExponent[f]);
+                    y[i] = unit_function(f, x0 + t[i] * width, beta);
                 }
                 lsq_fit(samples, order, t.data(), y.data(), a.data());
                 /* p(x) = sum_m a_m ((x - x0)/w)^m  ->  sum_k c_k x^k */

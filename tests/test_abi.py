@@ -39,7 +39,7 @@ def test_struct_layouts_match_header():
     mirror's."""
     text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "mdrl.h").read_text(), flags=re.S)
     for cname, cls in (("mdrl_params", m.Params), ("mdrl_stats", m.Stats), ("mdrl_replica", m.Replica),
-                       ("mdrl_tile", m.Tile)):
+                       ("mdrl_tile", m.Tile), ("mdrl_pme_params", m.PmeParams)):
         body = re.search(r"typedef struct \{((?:(?!typedef struct).)*?)\}\s*" + cname + ";", text, re.S).group(1)
         fields = []
         for decl in body.split(";"):
