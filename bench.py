@@ -204,7 +204,11 @@ def run_ours(args, rank, world, local, dist):
     # ---- tuned: int64 fixed point, autotuned tile -------------------------------------------
     ctx = m.Context(params)
     ctx.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
-    tune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile(), "ms": None, "default_ms": None}
+    if args.tile:
+        ctx.set_tile(*args.tile)
+        tune = {"tile": ctx.tile(), "ms": None, "default_ms": None}
+    else:
+        tune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile(), "ms": None, "default_ms": None}
     timed_steps(ctx, args.warmup)
     barrier()
     clocks = Clocks(local)
@@ -311,7 +315,7 @@ def run_ours(args, rank, world, local, dist):
                    "accumulation": "int64 fixed point 2^-24 (tuned)", "parallelism": f"replicas x{world}",
                    "tile": {"warps_per_cta": tune["tile"][0], "steps_per_piece": tune["tile"][1],
                             "prune_steps": tune["tile"][2],
-                            "autotuned": not args.no_tune, "force_ms_tuned": tune["ms"],
+                            "autotuned": not (args.no_tune or args.tile), "force_ms_tuned": tune["ms"],
                             "force_ms_default_tile": tune["default_ms"]},
                    "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
                    "pairs_per_step": pairs_launch},
@@ -516,6 +520,8 @@ def main():
     ap.add_argument("--order", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile (no autotuning)")
+    ap.add_argument("--tile", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
+                    help="fixed tile warps,steps,prune instead of autotuning (e.g. 4,6,1)")
     ap.add_argument("--pme", action="store_true", help="also time the step with smooth-PME electrostatics")
     ap.add_argument("--pme-order", type=int, default=4)
     args = ap.parse_args()

@@ -256,6 +256,9 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
     if (e == cudaSuccess) e = cudaEventCreate(&c->evf1);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_tot, sizeof(DevTotals));
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_mt, 2 * sizeof(MassTab));
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_mt, &c->mt_half, sizeof(MassTab), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_mt + 1, &c->mt_full, sizeof(MassTab), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, p->device);
     if (e != cudaSuccess) {
         set_error(std::string("context setup: ") + cudaGetErrorString(e));
@@ -289,7 +292,7 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
     free_particles(c);
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
-    dfree(&c->d_tot); dfree(&c->d_err);
+    dfree(&c->d_tot); dfree(&c->d_err); dfree(&c->d_mt);
     dfree(&c->d_pr); dfree(&c->d_pn); dfree(&c->d_pout); dfree(&c->d_ptr); dfree(&c->d_ptn); dfree(&c->d_paux);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -467,7 +470,7 @@ static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const floa
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     const bool energy = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, energy));
-    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (energy) MDRL_TRY(pme_add_energy(c, n));
     if (n > 0)
@@ -707,9 +710,9 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, extra));
-    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->mt_half, 0,
+    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->d_mt, 0,
                                                 c->d_kepart);
-    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());
@@ -725,7 +728,7 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     const int n = c->n;
     const int a = c->cur, b = 1 - c->cur;
     const bool vv = c->p.integrator == MDRL_INT_VELOCITY_VERLET;
-    const MassTab &mt = vv ? c->mt_half : c->mt_full;
+    const MassTab *mt = vv ? c->d_mt : c->d_mt + 1;
     const float dt = (float)c->p.dt_fs;
     MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
     k_kick_drift_bin<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pos[a], c->d_vel[a], c->d_type[a], c->d_F64,
@@ -742,9 +745,9 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[b], c->d_F64, c->d_F32, extra));
     /* kinetic energy only when energies are requested */
     if (vv || extra)
-        k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->mt_half,
+        k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->d_mt,
                                                     vv ? 1 : 0, extra ? c->d_kepart : nullptr);
-    k_totals<<<1, 256, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
                                        c->d_kepart, c->d_tot, extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());

@@ -64,14 +64,14 @@ __global__ void k_bbin_user(int n, const float *__restrict__ x, const float *__r
 /* v += F * cm[type], x += v * dt, wrap into the replica's box, bin. */
 __global__ void k_bkick_drift_bin(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                   const int *__restrict__ ptype, const unsigned long long *__restrict__ F64,
-                                  MassTab mt, float dt, const int *__restrict__ rep_of,
+                                  const MassTab *__restrict__ mt, float dt, const int *__restrict__ rep_of,
                                   const BatchRep *__restrict__ reps, int *__restrict__ cell_of,
                                   int *__restrict__ slot, int *__restrict__ count, unsigned *__restrict__ key) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const BatchRep &rp = reps[rep_of[k]];
     const Geom g = rp.g;
-    const float cm = mt.cm[ptype[k]];
+    const float cm = mt->cm[ptype[k]];
     float4 v = vel[k];
     float4 p = pos[k];
     v.x = __fmaf_rn(from_fixed(F64[k]), cm, v.x);
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(128) k_rep_totals(const int *__restrict__ item
                                                     const UnitOut *__restrict__ uout,
                                                     const BatchRep *__restrict__ reps,
                                                     const float4 *__restrict__ vel,
-                                                    const int *__restrict__ ptype, MassTab mt,
+                                                    const int *__restrict__ ptype, const MassTab *__restrict__ mt,
                                                     RepTotals *__restrict__ out) {
     __shared__ double s_d[128][4];
     __shared__ unsigned long long s_u[128][2];
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(128) k_rep_totals(const int *__restrict__ item
         const BatchRep &rp = reps[r];
         for (int e = t; e < rp.n; e += 128) {
             const float4 v = vel[rp.p_off + e];
-            const float m = mt.mass[ptype[rp.p_off + e]];
+            const float m = mt->mass[ptype[rp.p_off + e]];
             k += (double)(0.5f * m * (v.x * v.x + v.y * v.y + v.z * v.z) * (1.0f / 4.184e-4f));
         }
     }
@@ -404,7 +404,7 @@ extern "C" mdrl_status mdrl_batch_force_eval(mdrl_batch *b, const float *x, cons
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
     MDRL_TRY(batch_bin_user(b, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0));
     MDRL_TRY(batch_launch_force(b, c->d_pos[0], c->d_type[0], extra, c->d_F64));
-    k_totals<<<1, 256, 0, c->stream>>>(b->nitems, c->d_unit, 0, c->d_kepart, c->d_tot, extra ? 1 : 0);
+    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, 0, c->d_kepart, c->d_tot, extra ? 1 : 0);
     k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, nullptr, c->d_cnt, c->d_ox, c->d_oy,
                                                   c->d_oz, counts ? c->d_ocnt : nullptr);
     MDRL_CUDA(cudaGetLastError());
@@ -447,9 +447,9 @@ extern "C" mdrl_status mdrl_batch_set_state(mdrl_batch *b, const float *x, const
                                                       c->d_vel[0]);
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(batch_launch_force(b, c->d_pos[0], c->d_type[0], extra, c->d_F64));
-    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, nullptr, c->mt_half, 0,
+    k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, nullptr, c->d_mt, 0,
                                                 c->d_kepart);
-    k_totals<<<1, 256, 0, c->stream>>>(b->nitems, c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot, extra ? 1 : 0);
+    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot, extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_TRY(check_device_errors(c));
@@ -464,7 +464,7 @@ static mdrl_status batch_enqueue_step(mdrl_batch *b, bool extra) {
     const int n = b->ntot;
     const int a = c->cur, d = 1 - c->cur;
     const bool vv = c->p.integrator == MDRL_INT_VELOCITY_VERLET;
-    const MassTab &mt = vv ? c->mt_half : c->mt_full;
+    const MassTab *mt = vv ? c->d_mt : c->d_mt + 1;
     const float dt = (float)c->p.dt_fs;
     MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * (size_t)b->ncells, c->stream));
     k_bkick_drift_bin<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pos[a], c->d_vel[a], c->d_type[a], c->d_F64, mt,
@@ -479,9 +479,9 @@ static mdrl_status batch_enqueue_step(mdrl_batch *b, bool extra) {
     if (extra) MDRL_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * (size_t)n, c->stream));
     MDRL_TRY(batch_launch_force(b, c->d_pos[d], c->d_type[d], extra, c->d_F64));
     if (vv || extra)
-        k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[d], c->d_type[d], c->d_F64, nullptr, c->mt_half,
+        k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[d], c->d_type[d], c->d_F64, nullptr, c->d_mt,
                                                     vv ? 1 : 0, extra ? c->d_kepart : nullptr);
-    k_totals<<<1, 256, 0, c->stream>>>(b->nitems, c->d_unit, extra ? nblk(n, 256) : 0, c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, extra ? nblk(n, 256) : 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
@@ -555,7 +555,7 @@ extern "C" mdrl_status mdrl_batch_replica_stats(mdrl_batch *b, mdrl_stats *out) 
     const int a = c->cur;
     const bool kin = c->have_state;
     k_rep_totals<<<b->nrep, 128, 0, c->stream>>>(b->d_item_begin, b->d_rep_items, c->d_unit, b->d_reps,
-                                                 kin ? c->d_vel[a] : nullptr, c->d_type[a], c->mt_half,
+                                                 kin ? c->d_vel[a] : nullptr, c->d_type[a], c->d_mt,
                                                  b->d_reptot);
     MDRL_CUDA(cudaGetLastError());
     std::vector<RepTotals> h(b->nrep);

@@ -69,6 +69,7 @@ struct mdrl_ctx {
     float4 *d_fr = nullptr;      /* order 1: force functions packed per index (32 B) */
     float4 *d_pcoef = nullptr;
     MassTab mt_half, mt_full;
+    MassTab *d_mt = nullptr;     /* device copies: [0] half kick, [1] full kick */
 
     /* particle buffers */
     int cap = 0, n = 0;

@@ -46,6 +46,8 @@ __constant__ int c_halfshell[kHalfShellCells][3] = {
 /* Error bits raised by kernels and read by the host after a call. */
 enum : unsigned { kErrPosition = 1u, kErrType = 2u };
 
+/* Per-type mass factors, kept in device memory and read through a pointer (a by-value kernel
+ * parameter indexed by a particle's type would be copied to local memory in every thread). */
 struct MassTab {
     float cm[MDRL_MAX_TYPES];   /* velocity increment per unit force for the kick */
     float mass[MDRL_MAX_TYPES]; /* amu, for the kinetic energy */
@@ -189,7 +191,8 @@ __device__ __forceinline__ unsigned cell_morton(const Geom &g, float x, float y,
     unsigned q[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const float loc = (p[d] - (float)cc[d] * g.edge[d]) * (1024.0f / g.edge[d]);
+        /* an ordering only: the fast reciprocal (deterministic) is as good as an IEEE division */
+        const float loc = (p[d] - (float)cc[d] * g.edge[d]) * __fdividef(1024.0f, g.edge[d]);
         q[d] = (unsigned)min(1023, max(0, (int)loc));
     }
     return (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
@@ -267,28 +270,40 @@ static __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict_
                                                           const int *__restrict__ tmp,
                                                           int *__restrict__ sorted,
                                                           const unsigned *__restrict__ key) {
-    __shared__ unsigned long long s_k[1024];
+    __shared__ __align__(16) unsigned long long s_k[1024];
     const int c = blockIdx.x;
     const int s = start[c], m = start[c + 1] - s;
     if (m == 0) return;
-    const bool staged = m <= 1024;
-    if (staged) {
+    if (m <= 1024) {
         for (int e = threadIdx.x; e < m; e += blockDim.x) {
             const int id = tmp[s + e];
             s_k[e] = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id;
         }
+        if ((m & 1) && threadIdx.x == 0) s_k[m] = ~0ull;     /* pad to an even count: never smaller */
         __syncthreads();
+        const int m2 = (m + 1) >> 1;
+        const ulonglong2 *s_k2 = reinterpret_cast<const ulonglong2 *>(s_k);
+        for (int e = threadIdx.x; e < m; e += blockDim.x) {
+            const unsigned long long me = s_k[e];
+            /* rank = number of smaller keys; two keys per shared load, four independent counters */
+            int r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+            int q = 0;
+            for (; q + 1 < m2; q += 2) {
+                const ulonglong2 a = s_k2[q], b = s_k2[q + 1];
+                r0 += a.x < me; r1 += a.y < me; r2 += b.x < me; r3 += b.y < me;
+            }
+            if (q < m2) { const ulonglong2 a = s_k2[q]; r0 += a.x < me; r1 += a.y < me; }
+            sorted[s + r0 + r1 + r2 + r3] = (int)(me & 0xffffffffu);
+        }
+        return;
     }
     for (int e = threadIdx.x; e < m; e += blockDim.x) {
-        unsigned long long me;
-        if (staged) me = s_k[e];
-        else { const int id = tmp[s + e]; me = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id; }
+        const int ide = tmp[s + e];
+        const unsigned long long me = ((unsigned long long)(key ? key[ide] : 0u) << 32) | (unsigned)ide;
         int r = 0;
         for (int q = 0; q < m; ++q) {
-            unsigned long long o;
-            if (staged) o = s_k[q];
-            else { const int id = tmp[s + q]; o = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id; }
-            r += o < me;
+            const int id = tmp[s + q];
+            r += (((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id) < me;
         }
         sorted[s + r] = (int)(me & 0xffffffffu);
     }
@@ -318,41 +333,59 @@ static __global__ void k_gather_user(int n, const int *__restrict__ sorted, cons
     if (counts) counts[k] = 0;
 }
 
-/* Totals over units and kinetic-energy partials, in a fixed order (one CTA).  GB300 runs FP64 at
- * a small fraction of its FP32 rate, so the FP64 energy sums run only when energies were computed. */
-static __global__ void __launch_bounds__(256) k_totals(int nunits, const UnitOut *__restrict__ uout,
-                                                       int nke, const double *__restrict__ kepart,
-                                                       DevTotals *tot, int with_energy) {
-    __shared__ double s_d[256][4];
-    __shared__ unsigned long long s_u[256][2];
-    const int t = threadIdx.x;
+/* Totals over units and kinetic-energy partials, in a fixed order (one CTA of 1024 threads:
+ * strided partial sums, then warp shuffles and a final warp; the same order every call).  GB300
+ * runs FP64 at a small fraction of its FP32 rate, so the FP64 energy sums run only when energies
+ * were computed. */
+static __global__ void __launch_bounds__(1024) k_totals(int nunits, const UnitOut *__restrict__ uout,
+                                                        int nke, const double *__restrict__ kepart,
+                                                        DevTotals *tot, int with_energy) {
+    __shared__ double s_d[32][4];
+    __shared__ unsigned long long s_u[32][2];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     double a = 0, b = 0, c = 0, k = 0;
     unsigned long long p = 0, q = 0;
-    for (int u = t; u < nunits; u += 256) {
+    for (int u = t; u < nunits; u += 1024) {
         p += uout[u].pairs;
         if (with_energy) {
             a += uout[u].e_lj; b += uout[u].e_coul; c += uout[u].virial;
             q += uout[u].below;
         }
     }
-    for (int u = t; u < nke; u += 256) k += kepart[u];
-    s_d[t][0] = a; s_d[t][1] = b; s_d[t][2] = c; s_d[t][3] = k;
-    s_u[t][0] = p; s_u[t][1] = q;
-    __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
-        if (t < off) {
-            if (with_energy || nke > 0)
-                for (int m = 0; m < 4; ++m) s_d[t][m] += s_d[t + off][m];
-            s_u[t][0] += s_u[t + off][0];
-            s_u[t][1] += s_u[t + off][1];
+    for (int u = t; u < nke; u += 1024) k += kepart[u];
+    const bool fp = with_energy || nke > 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        p += __shfl_xor_sync(0xffffffffu, p, o);
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+        if (fp) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+            k += __shfl_xor_sync(0xffffffffu, k, o);
         }
-        __syncthreads();
     }
-    if (t == 0) {
-        tot->e_lj = s_d[0][0]; tot->e_coul = s_d[0][1]; tot->virial = s_d[0][2];
-        if (nke > 0) tot->kinetic = s_d[0][3];
-        tot->pairs = s_u[0][0]; tot->below = s_u[0][1];
-        tot->pairs_total += s_u[0][0];
+    if (lane == 0) { s_d[w][0] = a; s_d[w][1] = b; s_d[w][2] = c; s_d[w][3] = k; s_u[w][0] = p; s_u[w][1] = q; }
+    __syncthreads();
+    if (w != 0) return;
+    a = s_d[lane][0]; b = s_d[lane][1]; c = s_d[lane][2]; k = s_d[lane][3];
+    p = s_u[lane][0]; q = s_u[lane][1];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        p += __shfl_xor_sync(0xffffffffu, p, o);
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+        if (fp) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+            k += __shfl_xor_sync(0xffffffffu, k, o);
+        }
+    }
+    if (lane == 0) {
+        tot->e_lj = a; tot->e_coul = b; tot->virial = c;
+        if (nke > 0) tot->kinetic = k;
+        tot->pairs = p; tot->below = q;
+        tot->pairs_total += p;
     }
 }
 
@@ -398,12 +431,12 @@ __device__ __forceinline__ float force_of(const unsigned long long *F64, const f
 static __global__ void k_kick_drift_bin(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
                                  const int *__restrict__ ptype,
                                  const unsigned long long *__restrict__ F64,
-                                 const float *__restrict__ F32, MassTab mt, float dt, Geom g,
+                                 const float *__restrict__ F32, const MassTab *__restrict__ mt, float dt, Geom g,
                                  int *__restrict__ cell_of, int *__restrict__ slot,
                                  int *__restrict__ count, unsigned *__restrict__ key) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const float cm = mt.cm[ptype[k]];
+    const float cm = mt->cm[ptype[k]];
     float4 v = vel[k];
     float4 p = pos[k];
     v.x = __fmaf_rn(force_of(F64, F32, n, k, 0), cm, v.x);
@@ -445,7 +478,7 @@ static __global__ void k_gather_state(int n, const int *__restrict__ sorted,
  * (FP32 per particle and within the block, in a fixed order; FP64 across blocks). */
 static __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__ vel, const int *__restrict__ ptype,
                                                      const unsigned long long *__restrict__ F64,
-                                                     const float *__restrict__ F32, MassTab mt, int do_kick,
+                                                     const float *__restrict__ F32, const MassTab *__restrict__ mt, int do_kick,
                                                      double *__restrict__ kepart) {
     __shared__ float s_k[8];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -454,14 +487,14 @@ static __global__ void __launch_bounds__(256) k_kick(int n, float4 *__restrict__
         const int t = ptype[k];
         float4 v = vel[k];
         if (do_kick) {
-            const float cm = mt.cm[t];
+            const float cm = mt->cm[t];
             v.x = __fmaf_rn(force_of(F64, F32, n, k, 0), cm, v.x);
             v.y = __fmaf_rn(force_of(F64, F32, n, k, 1), cm, v.y);
             v.z = __fmaf_rn(force_of(F64, F32, n, k, 2), cm, v.z);
             vel[k] = v;
         }
         /* 1/2 m v^2 in kcal/mol with v in A/fs and m in amu: divide by 4.184e-4. */
-        if (kepart) ke = 0.5f * mt.mass[t] * (v.x * v.x + v.y * v.y + v.z * v.z) * (1.0f / 4.184e-4f);
+        if (kepart) ke = 0.5f * mt->mass[t] * (v.x * v.x + v.y * v.y + v.z * v.z) * (1.0f / 4.184e-4f);
     }
     if (!kepart) return;
 #pragma unroll
