@@ -256,6 +256,8 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
     if (e == cudaSuccess) e = cudaEventCreate(&c->evf1);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_tot, sizeof(DevTotals));
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_tot, sizeof(DevTotals));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_mt, 2 * sizeof(MassTab));
     if (e == cudaSuccess) e = cudaMemcpy(c->d_mt, &c->mt_half, sizeof(MassTab), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->d_mt + 1, &c->mt_full, sizeof(MassTab), cudaMemcpyHostToDevice);
@@ -293,6 +295,8 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
     dfree(&c->d_tot); dfree(&c->d_err); dfree(&c->d_mt);
+    if (c->h_tot) cudaFreeHost(c->h_tot);
+    if (c->h_err) cudaFreeHost(c->h_err);
     dfree(&c->d_pr); dfree(&c->d_pn); dfree(&c->d_pout); dfree(&c->d_ptr); dfree(&c->d_ptn); dfree(&c->d_paux);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -459,9 +463,12 @@ static mdrl_status read_stats(mdrl_ctx *c, mdrl_stats *st, float ms) {
     return MDRL_OK;
 }
 
-static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
-                                  const float *q, const int *type, float *fx, float *fy, float *fz,
-                                  int *counts, mdrl_stats *st) {
+/* One force evaluation enqueued on the context stream, ending with asynchronous copies of the
+ * error word and the totals into pinned host memory; force_eval_finish reads them after the one
+ * synchronisation of the call. */
+static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                      const float *q, const int *type, float *fx, float *fy, float *fz,
+                                      int *counts) {
     MDRL_TRY(ensure_capacity(c, n));
     const bool extra = counts != nullptr || (c->p.flags & MDRL_FLAG_ENERGY);
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
@@ -478,14 +485,49 @@ static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const floa
                                                       fz, counts);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
-    MDRL_CUDA(cudaStreamSynchronize(c->stream));
-    float ms = 0.0f;
-    MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    MDRL_TRY(check_device_errors(c));
-    MDRL_TRY(read_stats(c, st, ms));
-    if (st) st->candidates = -1;
+    MDRL_CUDA(cudaMemcpyAsync(c->h_tot, c->d_tot, sizeof(DevTotals), cudaMemcpyDeviceToHost, c->stream));
+    MDRL_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     c->have_state = false; /* the sorted buffers now hold this evaluation */
     return MDRL_OK;
+}
+
+static mdrl_status force_eval_finish(mdrl_ctx *c, mdrl_stats *st) {
+    const unsigned err = *c->h_err;
+    if (err & kErrPosition) {
+        set_error("positions must be finite and lie in [0, box) on every axis");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (err & kErrType) {
+        set_error("particle types must lie in [0, ntypes)");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (!st) return MDRL_OK;
+    const DevTotals &t = *c->h_tot;
+    memset(st, 0, sizeof(*st));
+    st->pairs = (int64_t)t.pairs;
+    st->candidates = -1;
+    st->below_table = (int64_t)t.below;
+    st->max_cell_occupancy = t.max_occ;
+    st->ncells = c->ncells;
+    st->e_lj = t.e_lj;
+    st->e_coul = t.e_coul;
+    st->virial = t.virial;
+    st->kinetic = t.kinetic;
+    st->pairs_total = (int64_t)t.pairs_total;
+    float ms = 0.0f, fms = 0.0f;
+    if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) st->device_ms = ms;
+    else cudaGetLastError();
+    if (cudaEventElapsedTime(&fms, c->evf0, c->evf1) == cudaSuccess) st->force_ms = fms;
+    else cudaGetLastError();
+    return MDRL_OK;
+}
+
+static mdrl_status force_eval_dev(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                  const float *q, const int *type, float *fx, float *fy, float *fz,
+                                  int *counts, mdrl_stats *st) {
+    MDRL_TRY(force_eval_enqueue(c, n, x, y, z, q, type, fx, fy, fz, counts));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    return force_eval_finish(c, st);
 }
 
 extern "C" mdrl_status mdrl_force_eval_device(mdrl_ctx *c, int n, const float *x, const float *y,
@@ -517,17 +559,17 @@ extern "C" mdrl_status mdrl_force_eval(mdrl_ctx *c, int n, const float *x, const
         if (q) MDRL_CUDA(cudaMemcpyAsync(c->d_uq, q, fb, cudaMemcpyHostToDevice, c->stream));
         if (type) MDRL_CUDA(cudaMemcpyAsync(c->d_ut, type, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     }
-    MDRL_TRY(force_eval_dev(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr,
-                            type ? c->d_ut : nullptr, c->d_ox, c->d_oy, c->d_oz,
-                            counts ? c->d_ocnt : nullptr, st));
+    MDRL_TRY(force_eval_enqueue(c, n, c->d_ux, c->d_uy, c->d_uz, q ? c->d_uq : nullptr,
+                                type ? c->d_ut : nullptr, c->d_ox, c->d_oy, c->d_oz,
+                                counts ? c->d_ocnt : nullptr));
     if (n > 0) {
         MDRL_CUDA(cudaMemcpyAsync(fx, c->d_ox, fb, cudaMemcpyDeviceToHost, c->stream));
         MDRL_CUDA(cudaMemcpyAsync(fy, c->d_oy, fb, cudaMemcpyDeviceToHost, c->stream));
         MDRL_CUDA(cudaMemcpyAsync(fz, c->d_oz, fb, cudaMemcpyDeviceToHost, c->stream));
         if (counts) MDRL_CUDA(cudaMemcpyAsync(counts, c->d_ocnt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     }
-    MDRL_CUDA(cudaStreamSynchronize(c->stream));
-    return MDRL_OK;
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));   /* the one synchronisation of the call */
+    return force_eval_finish(c, st);
 }
 
 extern "C" mdrl_status mdrl_bin(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,

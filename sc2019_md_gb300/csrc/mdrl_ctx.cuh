@@ -93,6 +93,8 @@ struct mdrl_ctx {
     double *d_kepart = nullptr;
     int kecap = 0;
     DevTotals *d_tot = nullptr;
+    DevTotals *h_tot = nullptr;  /* pinned host copies, read back with the results of a call */
+    unsigned *h_err = nullptr;
     unsigned *d_err = nullptr;
     int num_sms = 0;
 
