@@ -482,29 +482,6 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     }
                     float fjx = 0.f, fjy = 0.f, fjz = 0.f;
                     int cj = 0;
-#ifdef MDRL_FORCE_SPLIT
-                    /* filter phase: 8 independent r2 chains; force phase only for accepted pairs
-                     * (the differences are recomputed there with the same two roundings) */
-                    float r2k[8];
-                    unsigned okm = 0;
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
-                        const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
-                        const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
-                        r2k[k] = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                        bool ok = (r2k[k] > 0.0f) && (r2k[k] <= g.rc2);
-                        if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
-                        okm |= ok ? (1u << k) : 0u;
-                    }
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        if (okm & (1u << k)) {
-                            const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
-                            const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
-                            const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
-                            const float r2 = r2k[k];
-#else
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
@@ -515,7 +492,6 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                         bool ok = (r2 > 0.0f) && (r2 <= g.rc2);
                         if (diag) ok = ok && (ti * 32 + row + 4 * k < jl);
                         if (ok) {
-#endif
                             float v14, v8, v3, v12, v6, v1;
                             pair_functions_fast<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1);
                             const float4 pc = sCoef[tti[k] + ttj];

@@ -11,6 +11,7 @@
 import numpy as np
 import pytest
 
+import oracle
 import sc2019_md_gb300 as m
 from sc2019_md_gb300 import systems
 from helpers import oracle_from_ctx
@@ -193,3 +194,27 @@ def test_batch_errors(reps):
         with pytest.raises(m.MdrlError) as e:
             b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, tt)
         assert e.value.status == 1 and "types" in str(e.value)
+
+
+def test_batch512_full_size_pair_counts():
+    """The full batched workload (512 replicas, 2.52M atoms): every replica's pair count equals
+    the oracle's -- the half-shell traversal (multi-threaded restatement) for replicas with 3+
+    cells per axis, the all-image rule for the others -- and the batch total is their sum."""
+    reps = systems.batch512()
+    pos, vel, q, t, spec = systems.concat(reps)
+    p = reps[0].params(table_bins=512)
+    with m.Batch(p, spec) as b:
+        path = b.layout()["path"]
+        F, st, _ = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t)
+        rs = b.replica_stats()
+    assert np.isfinite(F).all()
+    assert st["pairs"] == sum(r["pairs"] for r in rs)
+    for r, s in enumerate(reps):
+        pc64 = oracle.lb_coefficients(s.sigma, s.epsilon)
+        o = oracle.System(s.pos, s.box, s.ncell, s.cutoff, pc64.astype(np.float32), q=s.q, type=s.type,
+                          ke=s.coulomb_k, eval=1, pcoef64=pc64, ke64=s.coulomb_k)
+        if path[r] == m.PATH_HALF_SHELL:
+            _, pairs = o.force_cells_mt()
+        else:
+            pairs = o.force_allimage()[4]["pairs"]
+        assert rs[r]["pairs"] == pairs, (r, s.n, int(path[r]), rs[r]["pairs"], pairs)
