@@ -129,6 +129,10 @@ typedef struct {
 const char *mdrl_version(void);
 const char *mdrl_last_error(void);
 
+/* The 14 half-shell cell offsets the force kernel traverses, offsets[14*3] = (dx, dy, dz), in the
+ * reference's filter order (home cell first); host only. */
+void mdrl_halfshell_offsets(int *offsets);
+
 /* Fill *p with defaults: 1 type of argon (sigma 3.4, epsilon 0.238, 39.95 amu), rc 8.5,
  * first-order 256-bin tables from 2^-2, FMA arithmetic, fixed-point accumulation,
  * velocity Verlet at 2 fs, device 0. */

@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 __all__ = [
-    "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables",
+    "Params", "Stats", "Context", "MdrlError", "lib", "library_path", "fit_tables", "halfshell_offsets",
     "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PmeParams", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
     "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
@@ -146,6 +146,8 @@ def lib() -> C.CDLL:
     L.mdrl_batch_get_state.argtypes = [vp, _F, _F, _F, _F, _F, _F, _F, _F, _F]
     L.mdrl_batch_replica_stats.argtypes = [vp, C.POINTER(Stats)]
     L.mdrl_batch_time_force.argtypes = [vp, _F]
+    L.mdrl_halfshell_offsets.argtypes = [_I]
+    L.mdrl_halfshell_offsets.restype = None
     L.mdrl_default_pme_params.argtypes = [C.POINTER(PmeParams)]
     L.mdrl_default_pme_params.restype = None
     L.mdrl_set_pme.argtypes = [vp, C.POINTER(PmeParams)]
@@ -215,6 +217,13 @@ def default_params(**kw) -> Params:
         else:
             setattr(p, k, v)
     return p
+
+
+def halfshell_offsets() -> np.ndarray:
+    """The 14 (dx, dy, dz) cell offsets of the half-shell traversal, home cell first (host only)."""
+    out = np.zeros((14, 3), dtype=np.int32)
+    lib().mdrl_halfshell_offsets(_ip(out))
+    return out
 
 
 def fit_tables(order: int, nseg: int, bins: int, min_log2: int, samples: int = 8) -> np.ndarray:

@@ -29,6 +29,11 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 
 extern "C" const char *mdrl_version(void) { return "mdrl 0.1 (sm_103a)"; }
 
+extern "C" void mdrl_halfshell_offsets(int *offsets) {
+    static const int t[kHalfShellCells][3] = MDRL_HALFSHELL_OFFSETS;
+    if (offsets) memcpy(offsets, t, sizeof(t));
+}
+
 extern "C" const char *mdrl_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" void mdrl_default_params(mdrl_params *p) {

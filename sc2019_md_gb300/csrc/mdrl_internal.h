@@ -23,6 +23,15 @@ constexpr int kThreads = kWarps * 32;
 constexpr int kChunk = 256;       /* particles of one cell staged in shared memory at a time */
 constexpr int kHalfShellCells = 14;
 
+/* The 14 cells a home cell pairs with, as (dx, dy, dz) cell offsets, in the reference's filter
+ * order (SC/Particle_Pair_Gen_HalfShell.v:14-24; MatlabScripts/FullScale_Simulation_LJArgon.m
+ * :381-749): in the reference's digits (2 = home, 1/3 = -1/+1) 222, 223, 231, 232, 233, 311, 312,
+ * 313, 321, 322, 323, 331, 332, 333; its 8 filters take 222 | 223 | 231 232 | 233 311 |
+ * 312 313 | 321 322 | 323 331 | 332 333.  The kernels' constant table is initialised from this. */
+#define MDRL_HALFSHELL_OFFSETS                                                                   \
+    {{0, 0, 0},  {0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 1},  {1, -1, -1}, {1, -1, 0},         \
+     {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},  {1, 1, -1}, {1, 1, 0},   {1, 1, 1}}
+
 /* Fixed-point force scale: 2^24 units per kcal/mol/Angstrom. */
 constexpr float kFixScale = 16777216.0f;
 constexpr float kFixInv = 5.9604644775390625e-8f;

@@ -38,10 +38,8 @@ struct TableDev {
     float r2min;
 };
 
-/* The 14 cells of the half shell in the reference's filter order (see oracle/oracle.cpp). */
-__constant__ int c_halfshell[kHalfShellCells][3] = {
-    {0, 0, 0},  {0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 1},  {1, -1, -1}, {1, -1, 0},
-    {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},  {1, 1, -1}, {1, 1, 0},   {1, 1, 1}};
+/* The 14 cells of the half shell in the reference's filter order (mdrl_internal.h). */
+__constant__ int c_halfshell[kHalfShellCells][3] = MDRL_HALFSHELL_OFFSETS;
 
 /* Error bits raised by kernels and read by the host after a call. */
 enum : unsigned { kErrPosition = 1u, kErrType = 2u };

@@ -19,6 +19,14 @@ except the .npz/.txt files it writes.
   cell_images_20k.json  SHA-256 and particle count of the 64 RTL cell-memory images
                    MatlabScripts/cell_ini_file_gen/cell_ini_file_{1..4}_{1..4}_{1..4}.{mif,hex}
                    (built by the reference from the same 20k positions, 7 x 6 x 6 cells of 8.5 A)
+  pair_stream_222.json  SHA-256 of a canonical form of MatlabScripts/VERIFICATION_PARTICLE_PAIR_INPUT.txt
+                   (the RTL pair generator's input stream for home cell (2,2,2) of the 20k LJArgon
+                   set: per reference particle and cycle the 8 filters' neighbour IDs, valid bits,
+                   the reference position and the valid neighbours' positions; invalid slots print
+                   stale reservoir data there and are left out), with its line count
+  energy_20k.json  step-1 energies of the reference golden model's 20k LJArgon runs
+                   (MatlabScripts/ICS19Results/{Double,Single,Interpolation}_PBC_20k.txt: potential,
+                   kinetic, total as printed; sigma 2.1 A, eps 1.995996^2, rc 8.5 A, 59.5 x 51 x 51 A)
   amber_dhfr.json  a digest of MatlabScripts/DHFR_23k_Input_Dataset/{prmtop,inpcrd}: file SHA-256,
                    pointers, box, net charge, the first atoms' fields and the 16 x 16 LJ A / B
                    (checked by the readers' tests when the reference tree is present)
@@ -192,8 +200,31 @@ def amber() -> None:
     print("amber:", out["pointers"]["NATOM"], "atoms")
 
 
+def pair_stream() -> None:
+    import hashlib
+    import json
+    sys.path.insert(0, str(REPO))
+    sys.path.insert(0, str(REPO / "tests"))
+    from helpers import pair_stream_canon_from_text
+    text = (MS / "VERIFICATION_PARTICLE_PAIR_INPUT.txt").read_bytes().decode()
+    canon = pair_stream_canon_from_text(text)
+    out = {"lines": len(canon), "sha256": hashlib.sha256("\n".join(canon).encode()).hexdigest()}
+    (HERE / "pair_stream_222.json").write_text(json.dumps(out, indent=0) + "\n")
+    print("pair_stream:", out["lines"], "lines")
+
+
+def energy_20k() -> None:
+    import json
+    out = {}
+    for name in ("Double", "Single", "Interpolation"):
+        f = (MS / "ICS19Results" / f"{name}_PBC_20k.txt").read_text().splitlines()[0].split()
+        out[name] = {"step": int(f[0]), "potential": float(f[1]), "kinetic": float(f[2]), "total": float(f[3])}
+    (HERE / "energy_20k.json").write_text(json.dumps(out, indent=0) + "\n")
+    print("energy_20k:", out["Double"])
+
+
 FIXTURES = {"kat1": kat1, "kat2": kat2, "kat3": kat3, "cmodel": cmodel, "cell_images": cell_images,
-            "amber": amber}
+            "amber": amber, "pair_stream": pair_stream, "energy_20k": energy_20k}
 
 if __name__ == "__main__":
     if not MS.exists():

@@ -53,3 +53,59 @@ def force_err(F, Fref):
     n = np.linalg.norm(Fref, axis=1)
     rms = np.sqrt((n ** 2).mean())
     return float(d.max() / rms), float(np.median(d / np.maximum(n, 1e-30)))
+
+
+# ---- the RTL pair generator's input stream (SC/Particle_Pair_Gen_HalfShell.v) -----------------
+# Its 8 filters take the half-shell cells in groups of 1, 1, 2, 2, 2, 2, 2, 2 (home first); a line
+# per reference particle of the home cell and cycle c holds, for filters 7..0, the c-th particle of
+# the filter's concatenated cell lists: "<cell digits><index %2X>" (digits 1/2/3 = -1/0/+1 about
+# the home cell, index 1-based in the cell), a valid bit, and positions as FP32 hex in z, y, x order.
+
+def _f32hex(v):
+    import struct
+    return "%08X" % struct.unpack(">I", struct.pack(">f", float(v)))[0]
+
+
+def pair_stream_canon_from_text(text):
+    """Canonical lines of VERIFICATION_PARTICLE_PAIR_INPUT.txt: every field but the positions of
+    invalid slots (which print stale reservoir data)."""
+    out = []
+    for line in text.replace("\r\n", "\n").split("\n")[1:]:
+        if not line:
+            continue
+        f = line.split("\t")
+        ids = [f[1][5 * s:5 * s + 5] for s in range(8)]
+        valid = f[2]
+        npos = [f[4][24 * s:24 * s + 24] if valid[s] == "1" else "-" for s in range(8)]
+        out.append("|".join([f[0]] + ids + [valid, f[3]] + npos))
+    return out
+
+
+def pair_stream_canon_from_cells(pos, cell_list, home, offsets):
+    """The same stream rebuilt from cell lists: cell_list(cx, cy, cz) (1-based) returns the particle
+    ids of a cell in cell order; offsets = the 14 half-shell offsets, home cell first."""
+    groups = [[0], [1], [2, 3], [4, 5], [6, 7], [8, 9], [10, 11], [12, 13]]
+    hexpos = lambda i: "".join(_f32hex(v) for v in pos[i][::-1])
+    filt = []
+    for g in groups:
+        lst = []
+        for o in g:
+            off = offsets[o]
+            code = "%d%d%d" % tuple(2 + int(off[d]) for d in range(3))
+            ids = cell_list(*(home[d] + int(off[d]) for d in range(3)))
+            lst += [(code + "%2X" % (k + 1), i) for k, i in enumerate(ids)]
+        filt.append(lst)
+    ncyc = max(len(l) for l in filt)
+    out = []
+    for k, a in enumerate(cell_list(*home)):
+        rid = "%d%d%d" % (2, 2, 2) + "%2X" % (k + 1)
+        for c in range(ncyc):
+            ids, valid, npos = [], "", []
+            for s in range(8):
+                lst = filt[7 - s]
+                if c < len(lst):
+                    ids.append(lst[c][0]); valid += "1"; npos.append(hexpos(lst[c][1]))
+                else:
+                    ids.append("000 0"); valid += "0"; npos.append("-")
+            out.append("|".join([rid] + ids + [valid, hexpos(a)] + npos))
+    return out
