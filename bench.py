@@ -17,6 +17,7 @@ cell-list port) on rank 0 with every host thread.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import ctypes as C
 import json
 import os
@@ -144,6 +145,20 @@ def measured_peaks() -> dict:
         except json.JSONDecodeError:
             pass
     return {}
+
+
+def committed_metric(workload: str, key: str):
+    """A figure of the committed ncu summary profiles/k_force_<workload>.md ("<key>: <value> ...")."""
+    f = ROOT / "profiles" / f"k_force_{workload}.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith(key + ":"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
 
 
 def committed_traffic(workload: str):
@@ -327,6 +342,7 @@ def run_ours(args, rank, world, local, dist):
                      "frac": achieved_tf / fp32_peak, "traffic": committed_traffic(args.workload),
                      "kernel": "k_force (half-shell pair force)", "force_ms": force_s * 1e3,
                      "flops_per_pair": FLOPS_PER_PAIR,
+                     "fma_pipe_active_pct_ncu": committed_metric(args.workload, "fma_pipe_active_pct"),
                      "peak_source": f"computed: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop x "
                                     f"{max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"},
         "roofline_hbm": {"achieved": alg_bytes / force_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
@@ -342,7 +358,7 @@ def run_ours(args, rank, world, local, dist):
         "wall_s": wall,
     }
     if world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"], out["force_error"] = cpu_baseline(sysm, params, args)
+        out["cpu_baseline"], out["force_error"], out["cpu_baseline_allpairs"] = cpu_baseline(sysm, params, args)
     return out
 
 
@@ -425,7 +441,8 @@ def run_batch(args, rank, world, local, dist):
         "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak, "traffic": committed_traffic("batch512"),
                      "kernel": "k_force (batched work list)",
-                     "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR},
+                     "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR,
+                     "fma_pipe_active_pct_ncu": committed_metric("batch512", "fma_pipe_active_pct")},
         "gpu_launches": 9 * args.steps,
         "clocks": clk,
     }
@@ -444,9 +461,18 @@ def oracle_system(sysm, order, bins, arith=0):
                          min_log2=m0, arith=arith, pcoef64=pc64, ke64=sysm.coulomb_k)
 
 
+def _force_error(F, Fref, vs):
+    d = np.linalg.norm(F - Fref, axis=1)
+    nrm = np.linalg.norm(Fref, axis=1)
+    return {"vs": vs, "max_over_rms": float(d.max() / np.sqrt((nrm ** 2).mean())),
+            "median_rel": float(np.median(d / np.maximum(nrm, 1e-30)))}
+
+
 def cpu_baseline(sysm, params, args):
-    """The oracle's multi-threaded cell-list port on the host cores (bounded sample), and the
-    force error of the GPU's first evaluation against the FP64 direct oracle."""
+    """The oracle's multi-threaded cell-list port on the host cores (bounded sample), a bounded
+    sample of the C model's all-pairs restatement, and the force error of the GPU's first
+    evaluation (tuned and plain) against the FP64 direct oracle and the FP64 evaluation of the
+    same tables."""
     import sc2019_md_gb300 as m
     o = oracle_system(sysm, params.table_order, params.table_bins)
     cores = os.cpu_count() or 1
@@ -461,14 +487,35 @@ def cpu_baseline(sysm, params, args):
     base = {"value": pairs / el, "unit": "pair-evals/s", "cores": cores, "kind": "port",
             "sample": f"{calls} full force evaluations of the same system (half-shell cell list, "
                       f"FP32, OpenMP over home cells)", "seconds": el}
+    # the C model's all-pairs O(N^2) form: every ordered pair of the first n_ap particles tested,
+    # the test rate extrapolated to the full system's N^2 tests and set against the pairs one
+    # cell-list evaluation of the full system finds
+    n_ap = min(sysm.n, 24000)
+    prefix = dataclasses.replace(sysm, pos=sysm.pos[:n_ap], vel=sysm.vel[:n_ap], type=sysm.type[:n_ap],
+                                 q=None if sysm.q is None else sysm.q[:n_ap])
+    sub = oracle_system(prefix, params.table_order, params.table_bins)
+    t1 = time.perf_counter()
+    sub.force_allpairs_mt(cores)
+    el_ap = time.perf_counter() - t1
+    tests_per_s = n_ap * n_ap / el_ap
+    full_s = float(sysm.n) ** 2 / tests_per_s
+    base_ap = {"value": (pairs / calls) / full_s, "unit": "pair-evals/s", "cores": cores, "kind": "port",
+               "sample": f"all {n_ap}^2 ordered pair tests of the first {n_ap} particles (C-model all-pairs "
+                         f"form, FP32, OpenMP over i), extrapolated to {sysm.n}^2 tests",
+               "pair_tests_per_s": tests_per_s, "full_eval_s": full_s, "seconds": el_ap}
     with m.Context(params) as ctx:
         F, _, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
+    pp = sysm.params(table_bins=params.table_bins, table_order=params.table_order, device=params.device,
+                     accum=m.ACC_FP32_ATOMIC)
+    with m.Context(pp) as ctx:
+        Fp, _, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
     F64, _ = o.force_direct64()
-    d = np.linalg.norm(F - F64, axis=1)
-    nrm = np.linalg.norm(F64, axis=1)
-    err = {"vs": "FP64 direct oracle, same pair set", "max_over_rms": float(d.max() / np.sqrt((nrm ** 2).mean())),
-           "median_rel": float(np.median(d / np.maximum(nrm, 1e-30)))}
-    return base, err
+    Ft, _ = o.force_tables64()
+    err = {"tuned": [_force_error(F, F64, "FP64 direct oracle, same pair set"),
+                     _force_error(F, Ft, "FP64 evaluation of the same tables")],
+           "plain": [_force_error(Fp, F64, "FP64 direct oracle, same pair set"),
+                     _force_error(Fp, Ft, "FP64 evaluation of the same tables")]}
+    return base, err, base_ap
 
 
 def run_reference(args, rank, world):
