@@ -277,7 +277,7 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
 }
 
 static void free_particles(mdrl_ctx *c) {
-    dfree(&c->d_ux); dfree(&c->d_uy); dfree(&c->d_uz); dfree(&c->d_uq); dfree(&c->d_ut);
+    dfree(&c->d_ux); dfree(&c->d_uy); dfree(&c->d_uz); dfree(&c->d_uq); dfree(&c->d_ut); dfree(&c->d_inv);
     dfree(&c->d_ox); dfree(&c->d_oy); dfree(&c->d_oz);
     dfree(&c->d_ovx); dfree(&c->d_ovy); dfree(&c->d_ovz); dfree(&c->d_ocnt);
     for (int b = 0; b < 2; ++b) { dfree(&c->d_pos[b]); dfree(&c->d_vel[b]); dfree(&c->d_type[b]); dfree(&c->d_id[b]); }
@@ -328,7 +328,7 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
     free_particles(c);
     const size_t m = (size_t)n;
     MDRL_TRY(dalloc(&c->d_ux, m)); MDRL_TRY(dalloc(&c->d_uy, m)); MDRL_TRY(dalloc(&c->d_uz, m));
-    MDRL_TRY(dalloc(&c->d_uq, m)); MDRL_TRY(dalloc(&c->d_ut, m));
+    MDRL_TRY(dalloc(&c->d_uq, m)); MDRL_TRY(dalloc(&c->d_ut, m)); MDRL_TRY(dalloc(&c->d_inv, m));
     MDRL_TRY(dalloc(&c->d_ox, m)); MDRL_TRY(dalloc(&c->d_oy, m)); MDRL_TRY(dalloc(&c->d_oz, m));
     MDRL_TRY(dalloc(&c->d_ovx, m)); MDRL_TRY(dalloc(&c->d_ovy, m)); MDRL_TRY(dalloc(&c->d_ovz, m));
     MDRL_TRY(dalloc(&c->d_ocnt, m));
@@ -412,13 +412,24 @@ static mdrl_status launch_force(mdrl_ctx *c, int n, const float4 *pos, const int
 /* Bin user-order arrays (already on the device) into the sorted buffers of slot `buf`.  With
  * `spatial` the cells are ordered by Morton key (the force path's order), otherwise by index
  * (the reference's in-cell order). */
+/* Bin user-order inputs into cell order (buffer buf).  stage: the inputs may be host memory the
+ * device reads directly; the binning pass copies them to the device staging buffers on the way
+ * and the gather reads those.  inv: also record each user index's cell-order position. */
 static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
-                            const float *q, const int *type, int buf, bool spatial) {
+                            const float *q, const int *type, int buf, bool spatial, bool stage = false,
+                            bool inv = false) {
     MDRL_CUDA(cudaMemsetAsync(c->d_count, 0, sizeof(int) * c->ncells, c->stream));
     MDRL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
     if (n > 0) {
-        k_bin_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, x, y, z, c->g, c->d_cell_of, c->d_slot,
-                                                        c->d_count, c->d_err, spatial ? c->d_key : nullptr);
+        k_bin_user<<<nblk(n, 256), 256, 0, c->stream>>>(
+            n, x, y, z, c->g, c->d_cell_of, c->d_slot, c->d_count, c->d_err, spatial ? c->d_key : nullptr,
+            stage ? q : nullptr, stage ? type : nullptr, stage ? c->d_ux : nullptr, c->d_uy, c->d_uz, c->d_uq,
+            c->d_ut);
+        if (stage) {
+            x = c->d_ux; y = c->d_uy; z = c->d_uz;
+            if (q) q = c->d_uq;
+            if (type) type = c->d_ut;
+        }
     }
     k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
     if (n > 0) {
@@ -427,7 +438,8 @@ static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, 
                                                        spatial ? c->d_key : nullptr);
         k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, x, y, z, q, type, c->d_pos[buf],
                                                            c->d_type[buf], c->d_id[buf], c->d_F64,
-                                                           c->d_F32, c->d_cnt, c->p.ntypes, c->d_err);
+                                                           c->d_F32, c->d_cnt, c->p.ntypes, c->d_err,
+                                                           inv ? c->d_inv : nullptr);
     }
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
@@ -468,17 +480,31 @@ static mdrl_status read_stats(mdrl_ctx *c, mdrl_stats *st, float ms) {
     return MDRL_OK;
 }
 
+/* The device address of p when the context's device can read and write it in place: page-locked
+ * host memory (cudaHostAlloc / cudaHostRegister, mapped), managed memory, or memory of this
+ * device; nullptr otherwise (pageable host memory: the caller stages through copies). */
+static void *mapped(const mdrl_ctx *c, const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice && a.device == c->p.device) return a.devicePointer;
+    return nullptr;
+}
+
 /* One force evaluation enqueued on the context stream, ending with asynchronous copies of the
  * error word and the totals into pinned host memory; force_eval_finish reads them after the one
  * synchronisation of the call. */
 static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
                                       const float *q, const int *type, float *fx, float *fy, float *fz,
-                                      int *counts) {
+                                      int *counts, bool stage = false) {
     MDRL_TRY(ensure_capacity(c, n));
     const bool extra = counts != nullptr || (c->p.flags & MDRL_FLAG_ENERGY);
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
-    MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0, true));
+    MDRL_TRY(bin_user(c, n, x, y, z, q, type, 0, true, stage, true));
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     const bool energy = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, energy));
@@ -486,8 +512,8 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
                                        extra ? 1 : 0);
     if (energy) MDRL_TRY(pme_add_energy(c, n));
     if (n > 0)
-        k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, c->d_F32, c->d_cnt, fx, fy,
-                                                      fz, counts);
+        k_unsort_inv<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_inv, c->d_F64, c->d_F32, c->d_cnt, fx, fy,
+                                                          fz, counts);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
     MDRL_CUDA(cudaMemcpyAsync(c->h_tot, c->d_tot, sizeof(DevTotals), cudaMemcpyDeviceToHost, c->stream));
@@ -556,6 +582,21 @@ extern "C" mdrl_status mdrl_force_eval(mdrl_ctx *c, int n, const float *x, const
     }
     MDRL_CUDA(cudaSetDevice(c->p.device));
     MDRL_TRY(ensure_capacity(c, n));
+    /* Pinned (page-locked) host buffers, or this device's memory: the kernels read the inputs and
+     * write the forces in place, coalesced, over the host link; no staging copies. */
+    if (n > 0) {
+        const void *dx = mapped(c, x), *dy = mapped(c, y), *dz = mapped(c, z);
+        void *dfx = mapped(c, fx), *dfy = mapped(c, fy), *dfz = mapped(c, fz);
+        const void *dq = q ? mapped(c, q) : nullptr, *dt = type ? mapped(c, type) : nullptr;
+        void *dc = counts ? mapped(c, counts) : nullptr;
+        if (dx && dy && dz && dfx && dfy && dfz && (!q || dq) && (!type || dt) && (!counts || dc)) {
+            MDRL_TRY(force_eval_enqueue(c, n, (const float *)dx, (const float *)dy, (const float *)dz,
+                                        (const float *)dq, (const int *)dt, (float *)dfx, (float *)dfy,
+                                        (float *)dfz, (int *)dc, true));
+            MDRL_CUDA(cudaStreamSynchronize(c->stream));   /* the one synchronisation of the call */
+            return force_eval_finish(c, st);
+        }
+    }
     const size_t fb = sizeof(float) * (size_t)n;
     if (n > 0) {
         MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));

@@ -75,6 +75,7 @@ struct mdrl_ctx {
     int cap = 0, n = 0;
     float *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_uq = nullptr;
     int *d_ut = nullptr;
+    int *d_inv = nullptr;   /* cell-order position of each user index (force evaluations) */
     float *d_ox = nullptr, *d_oy = nullptr, *d_oz = nullptr; /* user-order outputs */
     float *d_ovx = nullptr, *d_ovy = nullptr, *d_ovz = nullptr;
     int *d_ocnt = nullptr;

@@ -214,14 +214,26 @@ __device__ __forceinline__ int cell_slot(int *count, int c) {
     return base + rank;
 }
 
-/* Cell of each user-order particle, with its arrival slot in the cell. */
+/* Cell of each user-order particle, with its arrival slot in the cell.  With ux non-null the
+ * user arrays (which may be pinned host memory read over the host link) are also copied, in
+ * coalesced order, to device staging ux, uy, uz, uq (q given), ut (type given), so that the
+ * gather that follows reads device memory. */
 static __global__ void k_bin_user(int n, const float *__restrict__ x, const float *__restrict__ y,
                            const float *__restrict__ z, Geom g, int *__restrict__ cell_of,
                            int *__restrict__ slot, int *__restrict__ count,
-                           unsigned *__restrict__ err, unsigned *__restrict__ key) {
+                           unsigned *__restrict__ err, unsigned *__restrict__ key,
+                           const float *__restrict__ q = nullptr, const int *__restrict__ type = nullptr,
+                           float *__restrict__ ux = nullptr, float *__restrict__ uy = nullptr,
+                           float *__restrict__ uz = nullptr, float *__restrict__ uq = nullptr,
+                           int *__restrict__ ut = nullptr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float px = x[i], py = y[i], pz = z[i];
+    if (ux) {
+        ux[i] = px; uy[i] = py; uz[i] = pz;
+        if (q) uq[i] = q[i];
+        if (type) ut[i] = type[i];
+    }
     if (!in_box(g, px, py, pz)) atomicOr(err, kErrPosition);
     const int c = cell_of_pos(g, px, py, pz);
     cell_of[i] = c;
@@ -314,10 +326,11 @@ static __global__ void k_gather_user(int n, const int *__restrict__ sorted, cons
                               float4 *__restrict__ pos, int *__restrict__ ptype,
                               int *__restrict__ pid, unsigned long long *__restrict__ F64,
                               float *__restrict__ F32, int *__restrict__ counts, int ntypes,
-                              unsigned *__restrict__ err) {
+                              unsigned *__restrict__ err, int *__restrict__ inv = nullptr) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = sorted[k];
+    if (inv) inv[id] = k;
     pos[k] = make_float4(x[id], y[id], z[id], q ? q[id] : 0.0f);
     int t = type ? type[id] : 0;
     if (t < 0 || t >= ntypes) { atomicOr(err, kErrType); t = 0; }
@@ -395,6 +408,25 @@ static __global__ void k_unsort(int n, const int *__restrict__ pid, const unsign
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = pid[k];
+    if (F64) {
+        fx[id] = from_fixed(F64[k]); fy[id] = from_fixed(F64[n + k]); fz[id] = from_fixed(F64[2 * n + k]);
+    } else {
+        fx[id] = F32[k] + F32[3 * (size_t)n + k];
+        fy[id] = F32[n + k] + F32[4 * (size_t)n + k];
+        fz[id] = F32[2 * n + k] + F32[5 * (size_t)n + k];
+    }
+    if (cnt_u) cnt_u[id] = cnt_s[k];
+}
+
+/* The same in user order (inv = cell-order position of each user index): the writes are
+ * coalesced, so fx, fy, fz, cnt_u may be pinned host memory written over the host link. */
+static __global__ void k_unsort_inv(int n, const int *__restrict__ inv, const unsigned long long *__restrict__ F64,
+                                    const float *__restrict__ F32, const int *__restrict__ cnt_s,
+                                    float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ fz,
+                                    int *__restrict__ cnt_u) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int k = inv[id];
     if (F64) {
         fx[id] = from_fixed(F64[k]); fy[id] = from_fixed(F64[n + k]); fz[id] = from_fixed(F64[2 * n + k]);
     } else {

@@ -85,8 +85,10 @@ def test_bin_kat2_bit_exact():
     assert np.array_equal(order, oorder)
 
 
-def _check_force(sysm, params, tol=SUM_TOL):
+def _check_force(sysm, params, tol=SUM_TOL, tile=None):
     with m.Context(params) as ctx:
+        if tile is not None:
+            ctx.set_tile(*tile)
         x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
         F, st, cnt = ctx.force(x, y, z, sysm.q, sysm.type, counts=True)
         F2, st2, _ = ctx.force(x, y, z, sysm.q, sysm.type)
@@ -201,12 +203,14 @@ def test_edge_cases():
         m.Context(m.default_params(table_bins=300))
 
 
-def test_full_size_ljc92k_counts_and_forces():
-    """The 92,224-atom LJ+Coulomb system at full size: partner counts and pair total bit-equal to
-    the oracle, forces within the summation tolerance."""
+@pytest.mark.parametrize("tile", [None, (4, 6, 1), (8, 4, 1)])
+def test_full_size_ljc92k_counts_and_forces(tile):
+    """The 92,224-atom LJ+Coulomb system at full size, with the default tile and with pruned
+    (survivor-list) tiles: partner counts and pair total bit-equal to the oracle, forces within the
+    summation tolerance."""
     sysm = systems.ljc92k()
     p = sysm.params(table_bins=512)
-    F, Fo, o = _check_force(sysm, p)
+    F, Fo, o = _check_force(sysm, p, tile=tile)
 
 
 def test_full_size_ljc1m_pairs_and_reproducibility():
@@ -218,8 +222,11 @@ def test_full_size_ljc1m_pairs_and_reproducibility():
     with m.Context(p) as ctx:
         F1, st, _ = ctx.force(x, y, z, sysm.q, sysm.type)
         F2, _, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        ctx.set_tile(4, 6, 1)
+        _, st_pruned, _ = ctx.force(x, y, z, sysm.q, sysm.type)
         o = oracle_from_ctx(ctx, sysm)
     _, pairs = o.force_cells_mt(0)
     assert st["pairs"] == pairs
+    assert st_pruned["pairs"] == pairs
     assert np.array_equal(F1.view(np.uint32), F2.view(np.uint32))
     assert np.isfinite(F1).all()
