@@ -111,6 +111,7 @@ typedef struct {
     double device_ms;       /* device time of the last call, CUDA events */
     int64_t pairs_total;    /* pairs summed over every force evaluation of the last call */
     double force_ms;        /* device time of the last half-shell force kernel, CUDA events */
+    double e_bond, e_angle, e_dihedral; /* bonded-term energies, kcal/mol (MDRL_FLAG_ENERGY) */
 } mdrl_stats;
 
 typedef struct mdrl_ctx mdrl_ctx;
@@ -172,6 +173,26 @@ mdrl_status mdrl_get_pair_coefficients(mdrl_ctx *ctx, float *coef);
  * e.g. from an Amber topology's E = A/r^12 - B/r^6: A14 = 12A, B8 = -6B, A12 = A, B6 = -B.
  * The matrix should be symmetric for Newton's third law to hold. */
 mdrl_status mdrl_set_pair_coefficients(mdrl_ctx *ctx, const double *coef);
+
+/* Bonded terms, evaluated after the pair forces of every mdrl_force_eval / mdrl_set_state /
+ * mdrl_step and added to the same accumulators (replaces the reference's bonded engine,
+ * Bonded/Bonded_Top.v:57-396, whose forces its summation logic adds to the range-limited ones;
+ * per-term units Bonded/calc_bond_v2.v:16-127, calc_angle_v2.v:10-311, calcTorsion_v2.v:1-443,
+ * which take their parameters from the term packets documented at Bonded_Top.v:30-44).  Atoms are
+ * user indices.  Per term:
+ *   bond      atoms {i, j},       params {k, r0}:                E = k (r - r0)^2
+ *   angle     atoms {i, j, l},    params {k_theta, theta0, k_ub, s0} (j the vertex):
+ *             E = k_theta (theta - theta0)^2 + k_ub (|r_il| - s0)^2 (k_ub = 0: no Urey-Bradley)
+ *   dihedral  atoms {i, j, k, l}, params {k, n, delta}, n an integer in [0, 12]:
+ *             E = k (1 + cos(n phi + delta)) for n > 0, k (phi - delta)^2 (wrapped) for n = 0;
+ *             phi is the IUPAC dihedral (trans = pi); several terms may share atoms.
+ * Units kcal/mol, Angstrom, radian; vectors take the one-wrap periodic rule.  Terms are evaluated
+ * in FP32.  There are no non-bonded exclusions (the reference has none): bonded atoms also interact
+ * through the pair path.  Zero counts remove the terms.  Not available for replica batches. */
+mdrl_status mdrl_set_bonded(mdrl_ctx *ctx, int nbonds, const int *bond_atoms, const double *bond_params,
+                            int nangles, const int *angle_atoms, const double *angle_params,
+                            int ndihedrals, const int *dihedral_atoms, const double *dihedral_params);
+mdrl_status mdrl_get_bonded_counts(mdrl_ctx *ctx, int *nbonds, int *nangles, int *ndihedrals);
 
 /* Cell-list binning only (host arrays).  cell_of[n]: cell of each particle,
  * (cx*ny + cy)*nz + cz with c = floor(x / (box/ncell)); cell_count[ncells]; order[n]: particle

@@ -1,4 +1,4 @@
-"""ctypes wrapper of the CPU oracle (oracle.cpp).
+"""ctypes wrapper of the CPU oracle (oracle.cpp, bonded.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline / reference arm, as the checker or the timed CPU baseline.  The product package
@@ -25,6 +25,11 @@ class OrcSys(C.Structure):
         ("order", C.c_int), ("nseg", C.c_int), ("bins", C.c_int), ("min_log2", C.c_int),
         ("tab", _F), ("pcoef64", _D), ("ke64", C.c_double),
     ]
+
+
+class OrcBonded(C.Structure):
+    _fields_ = [("nb", C.c_int), ("bond_atoms", _I), ("bond_par", _D), ("na", C.c_int), ("angle_atoms", _I),
+                ("angle_par", _D), ("nd", C.c_int), ("dih_atoms", _I), ("dih_par", _D)]
 
 
 class OrcStats(C.Structure):
@@ -57,6 +62,7 @@ def lib() -> C.CDLL:
         L.orc_force_allimage.restype = C.c_int64
         L.orc_ewald64.argtypes = [C.POINTER(OrcSys), C.c_double, C.c_int, _D, _D]
         L.orc_cmodel_run.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, _F, _F, _F, _I]
+        L.orc_bonded64.argtypes = [C.c_int, _D, _D, _D, _D, C.POINTER(OrcBonded), _D, _D]
         _lib = L
     return _lib
 
@@ -224,3 +230,34 @@ def lb_coefficients(sigma, epsilon):
             eps = np.sqrt(epsilon[a] * epsilon[b])
             pc[a * T + b] = [48 * eps * sig ** 12, -24 * eps * sig ** 6, 4 * eps * sig ** 12, -4 * eps * sig ** 6]
     return pc
+
+
+def bonded64(pos, box=None, bonds=None, angles=None, dihedrals=None):
+    """FP64 bonded forces (n, 3) and energies {bond, angle, dihedral} (bonded.cpp).  Each term
+    set is (atoms (m, 2|3|4) int, params (m, 2|4|3) float): bonds {k, r0}; angles {k_theta,
+    theta0, k_ub, s0}; dihedrals {k, n, delta}.  box: periodic edges (None or 0: no wrap)."""
+    pos = np.asarray(pos, np.float64)
+    n = len(pos)
+    x, y, z = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    keep = []
+
+    def arr(t, w_atoms, w_par):
+        if t is None or len(t[0]) == 0:
+            return 0, None, None
+        a = np.ascontiguousarray(np.asarray(t[0], np.int32).reshape(-1, w_atoms))
+        p = np.ascontiguousarray(np.asarray(t[1], np.float64).reshape(-1, w_par))
+        assert len(a) == len(p)
+        keep.extend((a, p))
+        return len(a), _p(a, _I), _p(p, _D)
+
+    b = OrcBonded()
+    b.nb, b.bond_atoms, b.bond_par = arr(bonds, 2, 2)
+    b.na, b.angle_atoms, b.angle_par = arr(angles, 3, 4)
+    b.nd, b.dih_atoms, b.dih_par = arr(dihedrals, 4, 3)
+    bx = np.zeros(3) if box is None else np.asarray(box, np.float64)
+    F = np.zeros((n, 3))
+    E = np.zeros(3)
+    r = lib().orc_bonded64(n, _p(x, _D), _p(y, _D), _p(z, _D), _p(bx, _D), C.byref(b), _p(F, _D), _p(E, _D))
+    if r != 0:
+        raise ValueError(f"orc_bonded64: bad arguments ({r})")
+    return F, {"bond": E[0], "angle": E[1], "dihedral": E[2]}

@@ -1,4 +1,4 @@
-"""Build the CPU oracle (oracle/_build/liboracle.so) from oracle.cpp.
+"""Build the CPU oracle (oracle/_build/liboracle.so) from oracle.cpp and bonded.cpp.
 
 The oracle is test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline / reference arm load it.  -ffp-contract=off keeps every float expression rounded once
@@ -16,12 +16,12 @@ FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fas
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "oracle.cpp", HERE / "oracle.h"]
+    srcs = [HERE / "oracle.cpp", HERE / "bonded.cpp", HERE / "oracle.h"]
     if not force and LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in srcs):
         return LIB
     OUT.mkdir(parents=True, exist_ok=True)
     tmp = OUT / "liboracle.so.tmp"
-    cmd = ["g++", *FLAGS, str(HERE / "oracle.cpp"), "-o", str(tmp)]
+    cmd = ["g++", *FLAGS, str(HERE / "oracle.cpp"), str(HERE / "bonded.cpp"), "-o", str(tmp)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed: {' '.join(cmd)}\n{res.stderr}")

@@ -25,6 +25,9 @@
  *                      checker of the long-range (PME) path; no counterpart in the reference, whose
  *                      RL path truncates Coulomb at rc (its Long_Range/ RTL is a partial PME)
  *   orc_cmodel_run     SC/C_Model_ForceEval/MD_Evaluation_Model.cpp:57-203, expression by expression
+ *   orc_bonded64       (bonded.cpp) FP64 bond / angle + Urey-Bradley / dihedral terms as stated in
+ *                      Bonded/calc_bond_v2.v, calc_angle_v2.v, calcTorsion_v2.v (parity unpinned:
+ *                      the reference has no bonded golden values; checked by properties)
  *
  * Parity is pinned by the reference's own fixtures (tests/golden/, see make_golden.py) and by
  * the unmodified reference C model built under oracle/_ref (see build_ref.sh).
@@ -124,6 +127,27 @@ int orc_ewald64(const orc_sys *s, double beta, int nmax, double *F, double *ener
  * iteration; counts[n] (optional) the partner count of each particle in the last iteration. */
 int orc_cmodel_run(int n, int iters, float box, float cutoff, float *pos, float *vel,
                    float *energy, int *counts);
+
+/* Bonded terms (bonded.cpp).  Parameters per term: bond {k, r0} (E = k (r - r0)^2); angle
+ * {k_theta, theta0, k_ub, s0} (E = k_theta (theta - theta0)^2 + k_ub (d13 - s0)^2, atoms i-j-l
+ * with j the vertex); dihedral {k, n, delta} (E = k (1 + cos(n phi + delta)) for n > 0,
+ * k (phi - delta)^2 wrapped into [-pi, pi] for n = 0).  Units kcal/mol, Angstrom, radian. */
+typedef struct {
+    int nb;
+    const int *bond_atoms;     /* [2 nb] */
+    const double *bond_par;    /* [2 nb] */
+    int na;
+    const int *angle_atoms;    /* [3 na] */
+    const double *angle_par;   /* [4 na] */
+    int nd;
+    const int *dih_atoms;      /* [4 nd] */
+    const double *dih_par;     /* [3 nd] */
+} orc_bonded;
+
+/* FP64 bonded forces F[3n] (overwritten) and energies E[3] = {bonds, angles, dihedrals}; box
+ * edges > 0 wrap each difference once.  Returns 0, or < 0 on bad arguments / atom indices. */
+int orc_bonded64(int n, const double *x, const double *y, const double *z, const double box[3],
+                 const orc_bonded *b, double *F, double *E);
 
 #ifdef __cplusplus
 }

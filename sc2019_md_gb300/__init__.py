@@ -65,6 +65,7 @@ class Stats(C.Structure):
         ("max_cell_occupancy", C.c_int), ("ncells", C.c_int), ("e_lj", C.c_double),
         ("e_coul", C.c_double), ("virial", C.c_double), ("kinetic", C.c_double),
         ("device_ms", C.c_double), ("pairs_total", C.c_int64), ("force_ms", C.c_double),
+        ("e_bond", C.c_double), ("e_angle", C.c_double), ("e_dihedral", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -300,6 +301,32 @@ class Context:
         if c.size != self.params.ntypes ** 2 * 4:
             raise ValueError("coef must hold ntypes*ntypes*4 values")
         _check(lib().mdrl_set_pair_coefficients(self._h, c.ctypes.data_as(_D)))
+
+    def set_bonded(self, bonds=None, angles=None, dihedrals=None) -> None:
+        """Bonded terms (mdrl_set_bonded).  Each set is (atoms, params): bonds ((m, 2), (m, 2)
+        {k, r0}); angles ((m, 3), (m, 4) {k_theta, theta0, k_ub, s0}, the middle atom the vertex);
+        dihedrals ((m, 4), (m, 3) {k, n, delta}).  None everywhere removes the terms."""
+        keep = []
+
+        def arr(t, wa, wp):
+            if t is None or len(t[0]) == 0:
+                return 0, None, None
+            a = np.ascontiguousarray(np.asarray(t[0], dtype=np.int32).reshape(-1, wa))
+            p = np.ascontiguousarray(np.asarray(t[1], dtype=np.float64).reshape(-1, wp))
+            if len(a) != len(p):
+                raise ValueError("atoms and params differ in length")
+            keep.extend((a, p))
+            return len(a), _ip(a), p.ctypes.data_as(_D)
+
+        nb, ba, bp = arr(bonds, 2, 2)
+        na, aa, ap = arr(angles, 3, 4)
+        nd, da, dp = arr(dihedrals, 4, 3)
+        _check(lib().mdrl_set_bonded(self._h, nb, ba, bp, na, aa, ap, nd, da, dp))
+
+    def bonded_counts(self) -> tuple:
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().mdrl_get_bonded_counts(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def pair_coefficients(self) -> np.ndarray:
         T = self.params.ntypes

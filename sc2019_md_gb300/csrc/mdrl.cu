@@ -296,6 +296,7 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
     pme_free(c);
+    bonded_free(c);
     free_particles(c);
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
@@ -472,6 +473,9 @@ static mdrl_status read_stats(mdrl_ctx *c, mdrl_stats *st, float ms) {
     st->e_coul = t.e_coul;
     st->virial = t.virial;
     st->kinetic = t.kinetic;
+    st->e_bond = t.e_bond;
+    st->e_angle = t.e_angle;
+    st->e_dihedral = t.e_dihedral;
     st->device_ms = ms;
     st->pairs_total = (int64_t)t.pairs_total;
     float fms = 0.0f;
@@ -501,6 +505,7 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
                                       const float *q, const int *type, float *fx, float *fy, float *fz,
                                       int *counts, bool stage = false) {
     MDRL_TRY(ensure_capacity(c, n));
+    MDRL_TRY(bonded_check_atoms(c, n));
     const bool extra = counts != nullptr || (c->p.flags & MDRL_FLAG_ENERGY);
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
@@ -508,9 +513,11 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     const bool energy = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, energy));
+    MDRL_TRY(bonded_enqueue(c, n, c->d_pos[0], c->d_id[0], c->d_F64, c->d_F32, energy));
     k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (energy) MDRL_TRY(pme_add_energy(c, n));
+    if (energy) MDRL_TRY(bonded_add_energy(c, n));
     if (n > 0)
         k_unsort_inv<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_inv, c->d_F64, c->d_F32, c->d_cnt, fx, fy,
                                                           fz, counts);
@@ -544,6 +551,9 @@ static mdrl_status force_eval_finish(mdrl_ctx *c, mdrl_stats *st) {
     st->e_coul = t.e_coul;
     st->virial = t.virial;
     st->kinetic = t.kinetic;
+    st->e_bond = t.e_bond;
+    st->e_angle = t.e_angle;
+    st->e_dihedral = t.e_dihedral;
     st->pairs_total = (int64_t)t.pairs_total;
     float ms = 0.0f, fms = 0.0f;
     if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) st->device_ms = ms;
@@ -779,6 +789,7 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
     }
     MDRL_CUDA(cudaSetDevice(c->p.device));
     MDRL_TRY(ensure_capacity(c, n));
+    MDRL_TRY(bonded_check_atoms(c, n));
     const size_t fb = sizeof(float) * (size_t)n;
     MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));
     MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
@@ -798,11 +809,13 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(launch_force(c, n, c->d_pos[0], c->d_type[0], extra));
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, extra));
+    MDRL_TRY(bonded_enqueue(c, n, c->d_pos[0], c->d_id[0], c->d_F64, c->d_F32, extra));
     k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->d_mt, 0,
                                                 c->d_kepart);
     k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
+    if (extra) MDRL_TRY(bonded_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_TRY(check_device_errors(c));
@@ -831,6 +844,7 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     if (extra) MDRL_CUDA(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * (size_t)n, c->stream));
     MDRL_TRY(launch_force(c, n, c->d_pos[b], c->d_type[b], extra));
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[b], c->d_F64, c->d_F32, extra));
+    MDRL_TRY(bonded_enqueue(c, n, c->d_pos[b], c->d_id[b], c->d_F64, c->d_F32, extra));
     /* kinetic energy only when energies are requested */
     if (vv || extra)
         k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->d_mt,
@@ -838,6 +852,7 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
                                        c->d_kepart, c->d_tot, extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
+    if (extra) MDRL_TRY(bonded_add_energy(c, n));
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
 }

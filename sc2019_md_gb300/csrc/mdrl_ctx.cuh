@@ -16,6 +16,7 @@ using mdrl::set_error;
 
 namespace mdrl {
 struct PmeState;
+struct BondedState;
 }
 
 #define MDRL_CUDA(call)                                                                   \
@@ -114,6 +115,7 @@ struct mdrl_ctx {
 
     /* long-range electrostatics (mdrl_set_pme), null when off */
     mdrl::PmeState *pme = nullptr;
+    mdrl::BondedState *bonded = nullptr;   /* bonded terms (mdrl_set_bonded), or none */
 
     /* force-kernel tile (mdrl_set_tile / mdrl_autotune) */
     mdrl_tile tile = {mdrl::kFW, mdrl::kStepsPerPiece, 0};
@@ -132,6 +134,13 @@ mdrl_status pme_setup(mdrl_ctx *c, const mdrl_pme_params *p);
 void pme_free(mdrl_ctx *c);
 mdrl_status pme_enqueue(mdrl_ctx *c, int n, const float4 *pos, unsigned long long *F64, float *F32, bool energy);
 mdrl_status pme_add_energy(mdrl_ctx *c, int n);
+/* Bonded terms (mdrl_bonded.cu): forces into the accumulators of cell-order buffer pos / pid
+ * (after the pair kernel), energies into the totals (after k_totals). */
+mdrl_status bonded_enqueue(mdrl_ctx *c, int n, const float4 *pos, const int *pid, unsigned long long *F64,
+                           float *F32, bool energy);
+mdrl_status bonded_add_energy(mdrl_ctx *c, int n);
+mdrl_status bonded_check_atoms(const mdrl_ctx *c, int n);
+void bonded_free(mdrl_ctx *c);
 mdrl_status upload_tables(mdrl_ctx *c);
 /* Tiles: change (re-capturing graphs), and the autotuner's process-wide cache. */
 mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8);

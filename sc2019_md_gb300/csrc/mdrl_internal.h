@@ -57,6 +57,7 @@ struct DevTotals {
     unsigned long long pairs, below, pairs_total;
     int max_occ;
     int pad;
+    double e_bond, e_angle, e_dihedral;   /* bonded terms (zero without them) */
 };
 
 /* beta > 0: the Coulomb slots hold the Ewald real-space pair (erfc-screened) instead of r^-3, r^-1 */

@@ -394,6 +394,7 @@ static __global__ void __launch_bounds__(1024) k_totals(int nunits, const UnitOu
     }
     if (lane == 0) {
         tot->e_lj = a; tot->e_coul = b; tot->virial = c;
+        tot->e_bond = tot->e_angle = tot->e_dihedral = 0.0;   /* the bonded kernel adds its own */
         if (nke > 0) tot->kinetic = k;
         tot->pairs = p; tot->below = q;
         tot->pairs_total += p;

@@ -195,3 +195,66 @@ def concat(reps: list):
     q = np.concatenate([s.q for s in reps]).astype(np.float32)
     t = np.concatenate([s.type for s in reps]).astype(np.int32)
     return pos, vel, q, t, [(s.n, s.box) for s in reps]
+
+
+def chains(nchains: int, length: int, L: float, seed: int, cutoff: float = 10.0, bond: float = 1.53,
+           angle_deg: float = 111.0, dmin: float = 1.2, sigma: float = 1.0, epsilon: float = 0.05,
+           mass: float = 14.0):
+    """Linear chains of `length` beads grown in a periodic cube of edge L (bond `bond` A, bond
+    angle `angle_deg`, torsions drawn near 60/180/300 degrees, no two beads closer than dmin),
+    with harmonic bonds, angles (+ Urey-Bradley on every other angle) and 3-fold plus 1-fold
+    dihedral terms.  Returns (System, {"bonds": (atoms, params), "angles": ..., "dihedrals": ...});
+    the soft, small-sigma LJ keeps bonded neighbours (which also interact through the pair path)
+    well-behaved."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(seed)
+    th = np.deg2rad(angle_deg)
+    pos = []
+    for c in range(nchains):
+        for _ in range(1000):
+            chain = [rng.random(3) * L]
+            d = rng.standard_normal(3)
+            d /= np.linalg.norm(d)
+            while len(chain) < length:
+                if len(chain) == 1:
+                    nxt = chain[-1] + bond * d
+                else:
+                    b1 = chain[-1] - chain[-2]
+                    b1 /= np.linalg.norm(b1)
+                    u = np.cross(b1, rng.standard_normal(3))
+                    u /= np.linalg.norm(u)
+                    if len(chain) >= 3:
+                        b0 = chain[-2] - chain[-3]
+                        n0 = np.cross(b0, b1)
+                        n0 /= np.linalg.norm(n0)
+                        phi = np.deg2rad(rng.choice([60.0, 180.0, 300.0]) + rng.normal(0, 10))
+                        w = np.cross(b1, n0)
+                        u = np.cos(phi) * n0 + np.sin(phi) * w
+                    v = np.cos(np.pi - th) * b1 + np.sin(np.pi - th) * u
+                    nxt = chain[-1] + bond * v
+                chain.append(nxt)
+            cand = np.mod(np.array(chain), L)
+            allp = np.concatenate(pos + [cand]) if pos else cand
+            if len(cKDTree(allp, boxsize=L).query_pairs(dmin)) == 0:
+                pos.append(cand)
+                break
+        else:
+            raise RuntimeError("could not place the chains")
+    P = wrap_into_box(np.concatenate(pos), (L, L, L))
+    n = len(P)
+    idx = np.arange(n).reshape(nchains, length)
+    b_at = np.stack([idx[:, :-1].ravel(), idx[:, 1:].ravel()], 1)
+    b_par = np.tile([300.0, bond], (len(b_at), 1))
+    a_at = np.stack([idx[:, :-2].ravel(), idx[:, 1:-1].ravel(), idx[:, 2:].ravel()], 1)
+    a_par = np.tile([60.0, th, 0.0, 0.0], (len(a_at), 1))
+    a_par[::2, 2] = 20.0
+    a_par[::2, 3] = 2.0 * bond * np.sin(th / 2)
+    d1 = np.stack([idx[:, :-3].ravel(), idx[:, 1:-2].ravel(), idx[:, 2:-1].ravel(), idx[:, 3:].ravel()], 1)
+    d_at = np.concatenate([d1, d1])
+    d_par = np.concatenate([np.tile([1.4, 3, 0.0], (len(d1), 1)), np.tile([0.3, 1, np.pi], (len(d1), 1))])
+    m = np.full(n, mass)
+    cut = min(cutoff, L / 3)
+    nc = int(np.floor(np.float32(L) / np.float32(cut)))
+    sysm = System("chains", (L, L, L), cut, (nc, nc, nc), P, maxwell(n, m, 300.0, rng), None,
+                  np.zeros(n, np.int32), [sigma], [epsilon], [mass], 0.0)
+    return sysm, {"bonds": (b_at, b_par), "angles": (a_at, a_par), "dihedrals": (d_at, d_par)}
