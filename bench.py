@@ -193,6 +193,7 @@ def run_ours(args, rank, world, local, dist):
     import torch
 
     import sc2019_md_gb300 as m
+    from sc2019_md_gb300 import systems
 
     torch.cuda.set_device(local)
     sysm = make_system(args.workload, rank)
@@ -256,6 +257,29 @@ def run_ours(args, rank, world, local, dist):
                    "ns_per_day": (1000.0 / (ldev_ms / kl)) * params.dt_fs * 0.0864, "steps": kl,
                    "beta": pme_p["beta"], "grid": list(pme_p["grid"]), "order": pme_p["order"],
                    "note": "same step + PME reciprocal part (spread, 2 FFTs, gather); real space in the pair tables"}
+
+    # ---- bonded terms: their kernels alone, on a chain topology of the same size ------------
+    bonded_out = None
+    if not args.no_bonded:
+        nch = sysm.n // 30
+        Lc = float((nch * 30 / 0.1) ** (1.0 / 3.0))
+        csys, T = systems.chains(nch, 30, Lc, seed=20191117 + 6, cutoff=12.0, dmin=0.0)
+        ctxb = m.Context(csys.params(table_bins=args.bins, table_order=args.order, device=local))
+        ctxb.set_bonded(**T)
+        ctxb.set_state(csys.pos[:, 0], csys.pos[:, 1], csys.pos[:, 2], csys.vel, None, csys.type)
+        bms = []
+        for _ in range(max(3, min(args.steps, 20))):
+            flush.zero_()
+            torch.cuda.synchronize()
+            bms.append(ctxb.time_bonded())
+        ctxb.close()
+        nterms = sum(len(v[0]) for v in T.values())
+        bmed = float(np.median(bms))
+        bonded_out = {"terms": nterms, "bonds": len(T["bonds"][0]), "angles": len(T["angles"][0]),
+                      "dihedrals": len(T["dihedrals"][0]), "ms": bmed, "terms_per_s": nterms / (bmed * 1e-3),
+                      "workload": f"{csys.n} atoms as {nch} chains of 30 in a {Lc:.1f} A cube (density 0.1), "
+                                  f"FP32 terms into the int64 accumulators; kernels alone (inverse map + terms), "
+                                  f"L2 flushed"}
 
     # ---- plain: FP32 atomics, same tables --------------------------------------------------
     kp = max(3, min(args.steps, 50))
@@ -357,6 +381,7 @@ def run_ours(args, rank, world, local, dist):
                 "ms_per_call": e2e_s / ke * 1e3, "device_ms_per_call": e2e_dev / ke,
                 "host_link": "pinned buffers read and written in place by the binning and unsort kernels"},
         "with_pme": pme_out,
+        "bonded": bonded_out,
         "gpu_launches": 8 * args.steps,
         "clocks": clk,
         "wall_s": wall,
@@ -566,6 +591,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="ljc92k", choices=["ljc92k", "lj1728", "ljc1m", "batch512"])
+    ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term kernel timing")
     ap.add_argument("--replicas", type=int, default=512, help="batch512: number of replicas")
     ap.add_argument("--bins", type=int, default=512)
     ap.add_argument("--order", type=int, default=1)

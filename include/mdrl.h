@@ -186,13 +186,18 @@ mdrl_status mdrl_set_pair_coefficients(mdrl_ctx *ctx, const double *coef);
  *   dihedral  atoms {i, j, k, l}, params {k, n, delta}, n an integer in [0, 12]:
  *             E = k (1 + cos(n phi + delta)) for n > 0, k (phi - delta)^2 (wrapped) for n = 0;
  *             phi is the IUPAC dihedral (trans = pi); several terms may share atoms.
- * Units kcal/mol, Angstrom, radian; vectors take the one-wrap periodic rule.  Terms are evaluated
- * in FP32.  There are no non-bonded exclusions (the reference has none): bonded atoms also interact
+ * Units kcal/mol, Angstrom, radian; vectors take the one-wrap periodic rule (box edge taken off
+ * the far coordinate first).  Terms are evaluated in FP32, a bond's stretch r - r0 from a
+ * compensated r^2 - r0^2 so that stiff bonds at their rest length keep FP32 relative precision.
+ * There are no non-bonded exclusions (the reference has none): bonded atoms also interact
  * through the pair path.  Zero counts remove the terms.  Not available for replica batches. */
 mdrl_status mdrl_set_bonded(mdrl_ctx *ctx, int nbonds, const int *bond_atoms, const double *bond_params,
                             int nangles, const int *angle_atoms, const double *angle_params,
                             int ndihedrals, const int *dihedral_atoms, const double *dihedral_params);
 mdrl_status mdrl_get_bonded_counts(mdrl_ctx *ctx, int *nbonds, int *nangles, int *ndihedrals);
+/* Device time (ms, CUDA events) of one bonded-term launch on the current state, into scratch
+ * accumulators (the state is unchanged); 0 work without terms.  Needs mdrl_set_state. */
+mdrl_status mdrl_time_bonded(mdrl_ctx *ctx, float *ms);
 
 /* Cell-list binning only (host arrays).  cell_of[n]: cell of each particle,
  * (cx*ny + cy)*nz + cz with c = floor(x / (box/ncell)); cell_count[ncells]; order[n]: particle

@@ -323,6 +323,12 @@ class Context:
         nd, da, dp = arr(dihedrals, 4, 3)
         _check(lib().mdrl_set_bonded(self._h, nb, ba, bp, na, aa, ap, nd, da, dp))
 
+    def time_bonded(self) -> float:
+        """Device time (ms) of one launch of the bonded-term kernels on the current state."""
+        ms = C.c_float()
+        _check(lib().mdrl_time_bonded(self._h, C.byref(ms)))
+        return ms.value
+
     def bonded_counts(self) -> tuple:
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _check(lib().mdrl_get_bonded_counts(self._h, C.byref(a), C.byref(b), C.byref(c)))

@@ -18,7 +18,10 @@
  *   dihedral  E = k (1 + cos(n phi + delta)) (n > 0), k (phi - delta)^2 with the difference in
  *             [-pi, pi] (n = 0); phi is the IUPAC angle (ProtoMol's -atan2(c.b, a.b)); gradient of
  *             Blondel & Karplus, J. Comput. Chem. 17 (1996) 1132, which has no 1/sin(phi) factor.
- * Vectors between bonded atoms take the one-wrap periodic rule per axis.  Degenerate geometry (a
+ * Vectors between bonded atoms take the one-wrap periodic rule per axis, with the box edge taken
+ * off the far coordinate before the difference (bsub1), and a bond's stretch r - r0 comes from a
+ * compensated r^2 - r0^2 (norm2_hilo): FP32 terms, but a stiff bond at its rest length (water
+ * O-H, 553 kcal/mol/A^2 at 0.9572 A) keeps its force to FP32 precision.  Degenerate geometry (a
  * zero bond length, an angle within 1e-6 of 0 or pi in sine, collinear dihedral atoms) adds no
  * force.  Energies are summed per CTA in FP64 and over CTAs in a fixed order (k_bonded_energy).
  */
@@ -37,7 +40,7 @@ struct BondedState {
     int nb = 0, na = 0, nd = 0;
     int max_atom = -1;
     int2 *d_bi = nullptr;
-    float2 *d_bp = nullptr;   /* k, r0 */
+    float4 *d_bp = nullptr;   /* k, r0, hi and lo parts of r0^2 */
     int4 *d_ai = nullptr;     /* i, j (vertex), l */
     float4 *d_ap = nullptr;   /* k_theta, theta0, k_ub, s0 */
     int4 *d_di = nullptr;
@@ -49,7 +52,7 @@ struct BondedState {
 struct BondedDev {
     int nb, na, nd;
     const int2 *bi;
-    const float2 *bp;
+    const float4 *bp;
     const int4 *ai;
     const float4 *ap;
     const int4 *di;
@@ -61,9 +64,38 @@ static __global__ void k_invert(int n, const int *__restrict__ pid, int *__restr
     if (k < n) inv[pid[k]] = k;
 }
 
+/* a - b with the one-wrap rule decided on fl(a - b), but the box edge taken off the coordinate
+ * that lies beyond the half box before the two are subtracted: a - L is exact for a > L/2
+ * (Sterbenz), and the final difference is of two small numbers.  Subtracting L from fl(a - b)
+ * instead would keep the rounding of the difference of two far-apart coordinates (up to
+ * ulp(L)/2), which a stiff bond turns into a force error of 2 k ulp(L)/2. */
+__device__ __forceinline__ float bsub1(float a, float b, float L, float h) {
+    const float d = __fsub_rn(a, b);
+    if (d > h) return __fsub_rn(__fsub_rn(a, L), b);
+    if (d < -h) return __fsub_rn(a, __fsub_rn(b, L));
+    return d;
+}
 __device__ __forceinline__ float3 bsub(float4 a, float4 b, const Geom &g) {
-    return make_float3(wrap_d(__fsub_rn(a.x, b.x), g.L[0], g.h[0]), wrap_d(__fsub_rn(a.y, b.y), g.L[1], g.h[1]),
-                       wrap_d(__fsub_rn(a.z, b.z), g.L[2], g.h[2]));
+    return make_float3(bsub1(a.x, b.x, g.L[0], g.h[0]), bsub1(a.y, b.y, g.L[1], g.h[1]),
+                       bsub1(a.z, b.z, g.L[2], g.h[2]));
+}
+/* s + e = a + b exactly (Knuth's two-sum) */
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+/* r^2 of v as an unevaluated sum hi + lo (products split exactly with fma, the sum with two-sum):
+ * about twice FP32's precision, so that r^2 - r0^2 of a bond near its rest length keeps its digits */
+__device__ __forceinline__ float norm2_hilo(float3 v, float &lo) {
+    const float px = __fmul_rn(v.x, v.x), py = __fmul_rn(v.y, v.y), pz = __fmul_rn(v.z, v.z);
+    const float ex = __fmaf_rn(v.x, v.x, -px), ey = __fmaf_rn(v.y, v.y, -py), ez = __fmaf_rn(v.z, v.z, -pz);
+    float t1, t2;
+    const float s1 = two_sum(px, py, t1);
+    const float s = two_sum(s1, pz, t2);
+    lo = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), ex), ey), ez);
+    return s;
 }
 __device__ __forceinline__ float bdot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float3 bcross(float3 a, float3 b) {
@@ -85,11 +117,17 @@ k_bonded(BondedDev b, int n, const int *__restrict__ inv, const float4 *__restri
     float eb = 0.0f, ea = 0.0f, ed = 0.0f;
     if (t < b.nb) {
         const int2 at = b.bi[t];
-        const float2 p = b.bp[t];
+        const float4 p = b.bp[t];
         const int i = inv[at.x], j = inv[at.y];
         const float3 r = bsub(pos[i], pos[j], g);
-        const float d = sqrtf(bdot(r, r));
-        const float dd = d - p.y;
+        /* d - r0 = (d^2 - r0^2) / (d + r0) with d^2 and r0^2 (host, FP64) as hi + lo pairs: the
+         * difference of the hi parts is exact near the rest length, so the stretch of a stiff bond
+         * at equilibrium keeps FP32's relative precision instead of ulp(r0) */
+        float lo;
+        const float hi = norm2_hilo(r, lo);
+        const float d = sqrtf(hi);
+        const float den = __fadd_rn(d, p.y);   /* 0 only for d = r0 = 0 */
+        const float dd = den > 0.0f ? __fadd_rn(__fsub_rn(hi, p.z), __fsub_rn(lo, p.w)) / den : 0.0f;
         eb = p.x * dd * dd;
         if (d > 0.0f) {
             const float3 fi = bscale(-2.0f * p.x * dd / d, r);
@@ -309,10 +347,12 @@ extern "C" mdrl_status mdrl_set_bonded(mdrl_ctx *c, int nbonds, const int *bond_
     const long long nt = (long long)nbonds + nangles + ndihedrals;
     if (nt == 0) return MDRL_OK;
     std::vector<int2> bi(nbonds);
-    std::vector<float2> bp(nbonds);
+    std::vector<float4> bp(nbonds);
     for (int t = 0; t < nbonds; ++t) {
         bi[t] = make_int2(bond_atoms[2 * t], bond_atoms[2 * t + 1]);
-        bp[t] = make_float2((float)bond_params[2 * t], (float)bond_params[2 * t + 1]);
+        const double r0 = bond_params[2 * t + 1], r0sq = r0 * r0;
+        const float hi = (float)r0sq;
+        bp[t] = make_float4((float)bond_params[2 * t], (float)r0, hi, (float)(r0sq - (double)hi));
     }
     std::vector<int4> ai(nangles), di(ndihedrals);
     std::vector<float4> ap(nangles), dp(ndihedrals);
@@ -336,6 +376,25 @@ extern "C" mdrl_status mdrl_set_bonded(mdrl_ctx *c, int nbonds, const int *bond_
     MDRL_TRY(upload(&s->d_ai, ai)); MDRL_TRY(upload(&s->d_ap, ap));
     MDRL_TRY(upload(&s->d_di, di)); MDRL_TRY(upload(&s->d_dp, dp));
     MDRL_CUDA(cudaMalloc(&s->d_epart, sizeof(double) * 3 * (size_t)s->nblocks));
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_time_bonded(mdrl_ctx *c, float *ms) {
+    if (!c || !ms) { set_error("mdrl_time_bonded: null argument"); return MDRL_ERR_INVALID_ARG; }
+    if (!c->have_state) { set_error("mdrl_time_bonded: call mdrl_set_state first"); return MDRL_ERR_STATE; }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    const int n = c->n, a = c->cur;
+    /* scratch accumulators: the state's forces stay as they are */
+    const bool fp32 = c->p.accum != MDRL_ACC_FIXED64;
+    if (fp32 && !c->d_Fscr32) MDRL_TRY(dalloc(&c->d_Fscr32, 6 * (size_t)c->cap));
+    if (!fp32 && !c->d_Fscr64) MDRL_TRY(dalloc(&c->d_Fscr64, 3 * (size_t)c->cap));
+    if (fp32) MDRL_CUDA(cudaMemsetAsync(c->d_Fscr32, 0, sizeof(float) * 6 * (size_t)n, c->stream));
+    else MDRL_CUDA(cudaMemsetAsync(c->d_Fscr64, 0, sizeof(unsigned long long) * 3 * (size_t)n, c->stream));
+    MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
+    MDRL_TRY(bonded_enqueue(c, n, c->d_pos[a], c->d_id[a], c->d_Fscr64, c->d_Fscr32, false));
+    MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    MDRL_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
     return MDRL_OK;
 }
 

@@ -14,6 +14,7 @@ Readers
   read_amber_prmtop  Amber topology, both the fixed-order format without %FLAG sections
                      (MatlabScripts/DHFR_23k_Input_Dataset/prmtop) and the %FLAG format
   amber_nonbonded    per-atom type, charge (e) and mass, and the per-type-pair LJ A / B of a topology
+  amber_bonded       the topology's bonds, angles and dihedrals as mdrl_set_bonded terms
 
 Writers (the RTL cell-memory images, cell_ini_file_<x>_<y>_<z>.*)
   write_cell_mif     Altera MIF written by GenInputCellList_LJArgon.m:142-203: address 0 holds the
@@ -206,8 +207,9 @@ def _fixed_fields(lines, start, count, width, per_line, kind):
 def read_amber_prmtop(path) -> dict:
     """Sections of an Amber topology by their %FLAG names (both file formats): POINTERS (dict),
     ATOM_NAME, CHARGE, MASS, ATOM_TYPE_INDEX, NUMBER_EXCLUDED_ATOMS, NONBONDED_PARM_INDEX,
-    RESIDUE_LABEL, RESIDUE_POINTER, LENNARD_JONES_ACOEF, LENNARD_JONES_BCOEF (and, in the %FLAG
-    format, every other section)."""
+    RESIDUE_LABEL, RESIDUE_POINTER, the bond / angle / dihedral parameter tables, SOLTY,
+    LENNARD_JONES_ACOEF, LENNARD_JONES_BCOEF, BONDS_*, ANGLES_*, DIHEDRALS_* (with and without
+    hydrogen), EXCLUDED_ATOMS_LIST (and, in the %FLAG format, every other section)."""
     lines = Path(path).read_text().splitlines()
     if any(l.startswith("%FLAG") for l in lines[:10]):
         return _read_prmtop_flags(lines)
@@ -223,7 +225,13 @@ def read_amber_prmtop(path) -> dict:
              ("ANGLE_EQUIL_VALUE", P["NUMANG"], 16, 5, "e"), ("DIHEDRAL_FORCE_CONSTANT", P["NPTRA"], 16, 5, "e"),
              ("DIHEDRAL_PERIODICITY", P["NPTRA"], 16, 5, "e"), ("DIHEDRAL_PHASE", P["NPTRA"], 16, 5, "e"),
              ("SOLTY", P["NATYP"], 16, 5, "e"), ("LENNARD_JONES_ACOEF", t * (t + 1) // 2, 16, 5, "e"),
-             ("LENNARD_JONES_BCOEF", t * (t + 1) // 2, 16, 5, "e")]
+             ("LENNARD_JONES_BCOEF", t * (t + 1) // 2, 16, 5, "e"),
+             ("BONDS_INC_HYDROGEN", 3 * P["NBONH"], 6, 12, "i"), ("BONDS_WITHOUT_HYDROGEN", 3 * P["NBONA"], 6, 12, "i"),
+             ("ANGLES_INC_HYDROGEN", 4 * P["NTHETH"], 6, 12, "i"),
+             ("ANGLES_WITHOUT_HYDROGEN", 4 * P["NTHETA"], 6, 12, "i"),
+             ("DIHEDRALS_INC_HYDROGEN", 5 * P["NPHIH"], 6, 12, "i"),
+             ("DIHEDRALS_WITHOUT_HYDROGEN", 5 * P["NPHIA"], 6, 12, "i"),
+             ("EXCLUDED_ATOMS_LIST", P["NNB"], 6, 12, "i")]
     for name, count, width, per_line, kind in order:
         out[name], k = _fixed_fields(lines, k, count, width, per_line, kind)
     return out
@@ -270,6 +278,31 @@ def amber_nonbonded(prm: dict) -> dict:
     return {"ntypes": T, "type": np.asarray(prm["ATOM_TYPE_INDEX"], dtype=np.int32) - 1,
             "charge": np.asarray(prm["CHARGE"], dtype=np.float64) / AMBER_CHARGE_SCALE,
             "mass": np.asarray(prm["MASS"], dtype=np.float64), "A": A, "B": B}
+
+
+def amber_bonded(prm: dict) -> dict:
+    """The topology's bonded terms in mdrl_set_bonded's forms, terms with hydrogen first:
+    {'bonds': (atoms (m, 2), params (m, 2) {k, r0}), 'angles': (atoms (m, 3), params (m, 4)
+    {k, theta0, 0, 0}), 'dihedrals': (atoms (m, 4), params (m, 3) {k, n, delta})}.  Amber lists
+    atoms as 3 x (0-based index) and types 1-based; its E = PK (1 + cos(PN phi - PHASE)) is
+    k = PK, n = |PN|, delta = -PHASE here (the same IUPAC phi).  The signs Amber puts on the third
+    and fourth atoms (no 1-4 pair; improper) are dropped: there are no exclusions or 1-4 pairs
+    in the pair path.  SHAKE constraints are not applied: every bond is a harmonic term."""
+    def terms(with_h, without_h, width):
+        a = np.concatenate([np.asarray(prm.get(with_h, []), dtype=np.int64),
+                            np.asarray(prm.get(without_h, []), dtype=np.int64)]).reshape(-1, width)
+        return np.abs(a[:, :-1]) // 3, a[:, -1] - 1
+    ba, bt = terms("BONDS_INC_HYDROGEN", "BONDS_WITHOUT_HYDROGEN", 3)
+    aa, at = terms("ANGLES_INC_HYDROGEN", "ANGLES_WITHOUT_HYDROGEN", 4)
+    da, dt = terms("DIHEDRALS_INC_HYDROGEN", "DIHEDRALS_WITHOUT_HYDROGEN", 5)
+    f = lambda name: np.asarray(prm[name], dtype=np.float64)
+    bp = np.stack([f("BOND_FORCE_CONSTANT")[bt], f("BOND_EQUIL_VALUE")[bt]], axis=1)
+    ap = np.stack([f("ANGLE_FORCE_CONSTANT")[at], f("ANGLE_EQUIL_VALUE")[at], np.zeros(len(at)),
+                   np.zeros(len(at))], axis=1)
+    dp = np.stack([f("DIHEDRAL_FORCE_CONSTANT")[dt], np.abs(f("DIHEDRAL_PERIODICITY")[dt]),
+                   -f("DIHEDRAL_PHASE")[dt]], axis=1)
+    return {"bonds": (ba.astype(np.int32), bp), "angles": (aa.astype(np.int32), ap),
+            "dihedrals": (da.astype(np.int32), dp)}
 
 
 def pair_coefficients_from_AB(A: np.ndarray, B: np.ndarray) -> np.ndarray:

@@ -197,11 +197,32 @@ def concat(reps: list):
     return pos, vel, q, t, [(s.n, s.box) for s in reps]
 
 
+def _grow_chains(k: int, length: int, L: float, bond: float, th: float, rng) -> np.ndarray:
+    """k chains of `length` beads at once: (k, length, 3), bond length `bond`, bond angle th,
+    torsions near 60 / 180 / 300 degrees, first beads uniform in the cube [0, L)^3 (unwrapped)."""
+    unit = lambda v: v / np.linalg.norm(v, axis=-1, keepdims=True)
+    pos = np.zeros((k, length, 3))
+    pos[:, 0] = rng.random((k, 3)) * L
+    if length > 1:
+        pos[:, 1] = pos[:, 0] + bond * unit(rng.standard_normal((k, 3)))
+    for s in range(2, length):
+        b1 = unit(pos[:, s - 1] - pos[:, s - 2])
+        if s == 2:
+            u = unit(np.cross(b1, rng.standard_normal((k, 3))))
+        else:
+            n0 = unit(np.cross(pos[:, s - 2] - pos[:, s - 3], b1))
+            phi = np.deg2rad(rng.choice([60.0, 180.0, 300.0], k) + rng.normal(0, 10, k))[:, None]
+            u = np.cos(phi) * n0 + np.sin(phi) * np.cross(b1, n0)
+        pos[:, s] = pos[:, s - 1] + bond * (np.cos(np.pi - th) * b1 + np.sin(np.pi - th) * u)
+    return pos
+
+
 def chains(nchains: int, length: int, L: float, seed: int, cutoff: float = 10.0, bond: float = 1.53,
            angle_deg: float = 111.0, dmin: float = 1.2, sigma: float = 1.0, epsilon: float = 0.05,
            mass: float = 14.0):
     """Linear chains of `length` beads grown in a periodic cube of edge L (bond `bond` A, bond
-    angle `angle_deg`, torsions drawn near 60/180/300 degrees, no two beads closer than dmin),
+    angle `angle_deg`, torsions drawn near 60/180/300 degrees, no two beads closer than dmin;
+    dmin <= 0 skips that check, for large timing workloads),
     with harmonic bonds, angles (+ Urey-Bradley on every other angle) and 3-fold plus 1-fold
     dihedral terms.  Returns (System, {"bonds": (atoms, params), "angles": ..., "dihedrals": ...});
     the soft, small-sigma LJ keeps bonded neighbours (which also interact through the pair path)
@@ -210,36 +231,18 @@ def chains(nchains: int, length: int, L: float, seed: int, cutoff: float = 10.0,
     rng = np.random.default_rng(seed)
     th = np.deg2rad(angle_deg)
     pos = []
-    for c in range(nchains):
-        for _ in range(1000):
-            chain = [rng.random(3) * L]
-            d = rng.standard_normal(3)
-            d /= np.linalg.norm(d)
-            while len(chain) < length:
-                if len(chain) == 1:
-                    nxt = chain[-1] + bond * d
-                else:
-                    b1 = chain[-1] - chain[-2]
-                    b1 /= np.linalg.norm(b1)
-                    u = np.cross(b1, rng.standard_normal(3))
-                    u /= np.linalg.norm(u)
-                    if len(chain) >= 3:
-                        b0 = chain[-2] - chain[-3]
-                        n0 = np.cross(b0, b1)
-                        n0 /= np.linalg.norm(n0)
-                        phi = np.deg2rad(rng.choice([60.0, 180.0, 300.0]) + rng.normal(0, 10))
-                        w = np.cross(b1, n0)
-                        u = np.cos(phi) * n0 + np.sin(phi) * w
-                    v = np.cos(np.pi - th) * b1 + np.sin(np.pi - th) * u
-                    nxt = chain[-1] + bond * v
-                chain.append(nxt)
-            cand = np.mod(np.array(chain), L)
+    if dmin <= 0:
+        pos = [np.mod(c, L) for c in _grow_chains(nchains, length, L, bond, th, rng)]
+    for _ in range(1000):
+        if len(pos) == nchains:
+            break
+        for cand in _grow_chains(nchains - len(pos), length, L, bond, th, rng):
+            cand = np.mod(cand, L)
             allp = np.concatenate(pos + [cand]) if pos else cand
             if len(cKDTree(allp, boxsize=L).query_pairs(dmin)) == 0:
                 pos.append(cand)
-                break
-        else:
-            raise RuntimeError("could not place the chains")
+    if len(pos) < nchains:
+        raise RuntimeError("could not place the chains")
     P = wrap_into_box(np.concatenate(pos), (L, L, L))
     n = len(P)
     idx = np.arange(n).reshape(nchains, length)

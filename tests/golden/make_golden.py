@@ -27,6 +27,9 @@ except the .npz/.txt files it writes.
   energy_20k.json  step-1 energies of the reference golden model's 20k LJArgon runs
                    (MatlabScripts/ICS19Results/{Double,Single,Interpolation}_PBC_20k.txt: potential,
                    kinetic, total as printed; sigma 2.1 A, eps 1.995996^2, rc 8.5 A, 59.5 x 51 x 51 A)
+  dhfr_bonded.npz  the bonded terms of MatlabScripts/DHFR_23k_Input_Dataset/prmtop as
+                   formats.amber_bonded returns them (atoms, parameter-type index, parameter table)
+                   and the inpcrd positions wrapped into the 62.23 A box (FP32)
   amber_dhfr.json  a digest of MatlabScripts/DHFR_23k_Input_Dataset/{prmtop,inpcrd}: file SHA-256,
                    pointers, box, net charge, the first atoms' fields and the 16 x 16 LJ A / B
                    (checked by the readers' tests when the reference tree is present)
@@ -223,8 +226,30 @@ def energy_20k() -> None:
     print("energy_20k:", out["Double"])
 
 
+def dhfr_bonded() -> None:
+    """The DHFR topology's bonded terms (via formats.amber_bonded: atoms, 0-based parameter-type
+    index, the parameter tables) and the inpcrd positions wrapped into the box as FP32."""
+    sys.path.insert(0, str(REPO))
+    from sc2019_md_gb300 import formats as F
+    d = MS / "DHFR_23k_Input_Dataset"
+    prm = F.read_amber_prmtop(d / "prmtop")
+    crd = F.read_amber_inpcrd(d / "inpcrd")
+    b = F.amber_bonded(prm)
+    from sc2019_md_gb300 import systems
+    out = {"box": np.asarray(crd["box"][:3], np.float64)}
+    L = out["box"]
+    out["pos"] = systems.wrap_into_box(np.mod(np.asarray(crd["pos"], np.float64), L), tuple(L))
+    for name, (atoms, params) in b.items():
+        table, idx = np.unique(params, axis=0, return_inverse=True)
+        out[f"{name}_atoms"] = atoms.astype(np.int32)
+        out[f"{name}_type"] = idx.reshape(-1).astype(np.int16)
+        out[f"{name}_table"] = table
+    np.savez_compressed(HERE / "dhfr_bonded.npz", **out)
+    print("dhfr_bonded:", {k: v.shape for k, v in out.items()})
+
+
 FIXTURES = {"kat1": kat1, "kat2": kat2, "kat3": kat3, "cmodel": cmodel, "cell_images": cell_images,
-            "amber": amber, "pair_stream": pair_stream, "energy_20k": energy_20k}
+            "amber": amber, "pair_stream": pair_stream, "energy_20k": energy_20k, "dhfr_bonded": dhfr_bonded}
 
 if __name__ == "__main__":
     if not MS.exists():

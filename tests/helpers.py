@@ -109,3 +109,11 @@ def pair_stream_canon_from_cells(pos, cell_list, home, offsets):
                     ids.append("000 0"); valid += "0"; npos.append("-")
             out.append("|".join([rid] + ids + [valid, hexpos(a)] + npos))
     return out
+
+
+def dhfr_bonded():
+    """The DHFR (23,558 atoms) bonded terms and FP32 positions in the box, from the fixture:
+    (pos (n, 3) float32, box (3,), {"bonds": (atoms, params), "angles": ..., "dihedrals": ...})."""
+    d = np.load(GOLDEN / "dhfr_bonded.npz")
+    terms = {k: (d[f"{k}_atoms"], d[f"{k}_table"][d[f"{k}_type"]]) for k in ("bonds", "angles", "dihedrals")}
+    return d["pos"], tuple(float(v) for v in d["box"]), terms

@@ -73,7 +73,13 @@ def _synthetic_topology():
     return {"NATOM": 5, "NTYPES": 2, "NRES": 2, "names": ["OW", "HW1", "HW2", "AR", "AR"],
             "charge_e": [-0.834, 0.417, 0.417, 0.0, 0.0], "mass": [16.0, 1.008, 1.008, 39.948, 39.948],
             "type": [1, 2, 2, 1, 1], "numex": [2, 1, 0, 0, 0], "ico": [1, 2, 2, 3],
-            "acoef": [582000.0, 0.0, 0.0], "bcoef": [595.0, 0.0, 0.0], "labels": ["WAT", "AR"], "ptr": [1, 4]}
+            "acoef": [582000.0, 0.0, 0.0], "bcoef": [595.0, 0.0, 0.0], "labels": ["WAT", "AR"], "ptr": [1, 4],
+            # bonded sections: Amber lists atoms as 3 x index, types 1-based; a negative third /
+            # fourth dihedral atom flags "no 1-4" / "improper"
+            "rk": [553.0, 10.0], "req": [0.9572, 3.8], "tk": [100.0], "teq": [1.824],
+            "pk": [1.4, 10.5], "pn": [3.0, 2.0], "phase": [0.0, 3.14159400],
+            "bonh": [0, 3, 1, 0, 6, 1], "bona": [9, 12, 2], "theth": [3, 0, 6, 1], "theta": [],
+            "phih": [], "phia": [3, 0, -9, 12, 1, 6, 0, 9, -12, 2], "natex": [2, 3, 0]}
 
 
 def _fmt(vals, kind, width, per_line):
@@ -88,31 +94,53 @@ def _fmt(vals, kind, width, per_line):
     return out
 
 
-def _write_old(path, t):
+def _pointers(t):
     ptr = [0] * 30
     ptr[0], ptr[1], ptr[11] = t["NATOM"], t["NTYPES"], t["NRES"]
-    ptr[15] = ptr[16] = ptr[17] = ptr[18] = 1          # one bond / angle / dihedral type, one solty
+    ptr[2], ptr[4], ptr[6] = len(t["bonh"]) // 3, len(t["theth"]) // 4, len(t["phih"]) // 5
+    ptr[3] = ptr[12] = len(t["bona"]) // 3
+    ptr[5] = ptr[13] = len(t["theta"]) // 4
+    ptr[7] = ptr[14] = len(t["phia"]) // 5
+    ptr[10] = len(t["natex"])
+    ptr[15], ptr[16], ptr[17], ptr[18] = len(t["rk"]), len(t["tk"]), len(t["pk"]), 1
+    return ptr
+
+
+def _write_old(path, t):
+    ptr = _pointers(t)
     q = [c * F.AMBER_CHARGE_SCALE for c in t["charge_e"]]
     lines = [" " * 80] + _fmt(ptr, "i", 6, 12) + _fmt(t["names"], "a", 4, 20) + _fmt(q, "e", 16, 5) + \
         _fmt(t["mass"], "e", 16, 5) + _fmt(t["type"], "i", 6, 12) + _fmt(t["numex"], "i", 6, 12) + \
         _fmt(t["ico"], "i", 6, 12) + _fmt(t["labels"], "a", 4, 20) + _fmt(t["ptr"], "i", 6, 12)
-    for _ in range(8):                                  # RK REQ TK TEQ PK PN PHASE SOLTY
-        lines += _fmt([1.0], "e", 16, 5)
+    for key in ("rk", "req", "tk", "teq", "pk", "pn", "phase"):
+        lines += _fmt(t[key], "e", 16, 5)
+    lines += _fmt([1.0], "e", 16, 5)                   # SOLTY
     lines += _fmt(t["acoef"], "e", 16, 5) + _fmt(t["bcoef"], "e", 16, 5)
+    for key in ("bonh", "bona", "theth", "theta", "phih", "phia", "natex"):
+        lines += _fmt(t[key], "i", 6, 12)
     Path(path).write_text("\n".join(lines) + "\n")
 
 
 def _write_flags(path, t):
-    ptr = [0] * 30
-    ptr[0], ptr[1], ptr[11] = t["NATOM"], t["NTYPES"], t["NRES"]
+    ptr = _pointers(t)
     q = [c * F.AMBER_CHARGE_SCALE for c in t["charge_e"]]
     sec = [("POINTERS", "10I8", ptr, "i", 8, 10), ("ATOM_NAME", "20a4", t["names"], "a", 4, 20),
            ("CHARGE", "5E16.8", q, "e", 16, 5), ("MASS", "5E16.8", t["mass"], "e", 16, 5),
            ("ATOM_TYPE_INDEX", "10I8", t["type"], "i", 8, 10),
            ("NONBONDED_PARM_INDEX", "10I8", t["ico"], "i", 8, 10),
            ("RESIDUE_LABEL", "20a4", t["labels"], "a", 4, 20), ("RESIDUE_POINTER", "10I8", t["ptr"], "i", 8, 10),
+           ("BOND_FORCE_CONSTANT", "5E16.8", t["rk"], "e", 16, 5), ("BOND_EQUIL_VALUE", "5E16.8", t["req"], "e", 16, 5),
+           ("ANGLE_FORCE_CONSTANT", "5E16.8", t["tk"], "e", 16, 5), ("ANGLE_EQUIL_VALUE", "5E16.8", t["teq"], "e", 16, 5),
+           ("DIHEDRAL_FORCE_CONSTANT", "5E16.8", t["pk"], "e", 16, 5),
+           ("DIHEDRAL_PERIODICITY", "5E16.8", t["pn"], "e", 16, 5), ("DIHEDRAL_PHASE", "5E16.8", t["phase"], "e", 16, 5),
            ("LENNARD_JONES_ACOEF", "5E16.8", t["acoef"], "e", 16, 5),
-           ("LENNARD_JONES_BCOEF", "5E16.8", t["bcoef"], "e", 16, 5)]
+           ("LENNARD_JONES_BCOEF", "5E16.8", t["bcoef"], "e", 16, 5),
+           ("BONDS_INC_HYDROGEN", "10I8", t["bonh"], "i", 8, 10), ("BONDS_WITHOUT_HYDROGEN", "10I8", t["bona"], "i", 8, 10),
+           ("ANGLES_INC_HYDROGEN", "10I8", t["theth"], "i", 8, 10),
+           ("ANGLES_WITHOUT_HYDROGEN", "10I8", t["theta"], "i", 8, 10),
+           ("DIHEDRALS_INC_HYDROGEN", "10I8", t["phih"], "i", 8, 10),
+           ("DIHEDRALS_WITHOUT_HYDROGEN", "10I8", t["phia"], "i", 8, 10),
+           ("EXCLUDED_ATOMS_LIST", "10I8", t["natex"], "i", 8, 10)]
     lines = ["%VERSION  VERSION_STAMP = V0001.000  DATE = 01/01/20  00:00:00"]
     for name, fm, vals, kind, w, pl in sec:
         lines += [f"%FLAG {name}", f"%FORMAT({fm})"] + _fmt(vals, kind, w, pl)
@@ -130,6 +158,13 @@ def test_amber_prmtop_both_formats(tmp_path, writer):
     assert np.allclose(nb["charge"], t["charge_e"], rtol=0, atol=1e-8)
     assert list(nb["type"]) == [0, 1, 1, 0, 0]
     assert nb["A"][0, 0] == 582000.0 and nb["B"][0, 0] == 595.0 and nb["A"][1, 1] == 0.0
+    b = F.amber_bonded(prm)
+    assert b["bonds"][0].tolist() == [[0, 1], [0, 2], [3, 4]]
+    assert np.allclose(b["bonds"][1], [[553.0, 0.9572], [553.0, 0.9572], [10.0, 3.8]])
+    assert b["angles"][0].tolist() == [[1, 0, 2]] and np.allclose(b["angles"][1], [[100.0, 1.824, 0, 0]])
+    assert b["dihedrals"][0].tolist() == [[1, 0, 3, 4], [2, 0, 3, 4]]
+    assert np.allclose(b["dihedrals"][1], [[1.4, 3.0, 0.0], [10.5, 2.0, -3.141594]])
+    assert prm["EXCLUDED_ATOMS_LIST"] == t["natex"]
 
 
 def test_amber_inpcrd(tmp_path):
@@ -163,6 +198,23 @@ def test_amber_dhfr_matches_digest():
         assert prm["ATOM_NAME"][i] == a["name"] and int(nb["type"][i]) == a["type"]
         assert list(crd["pos"][i]) == a["pos"] and list(crd["vel"][i]) == a["vel"]
     assert len(crd["pos"]) == d["pointers"]["NATOM"] == 23558
+
+
+@pytest.mark.skipif(not DHFR.exists(), reason="reference tree not mounted")
+def test_amber_dhfr_bonded_matches_fixture():
+    """formats.amber_bonded on the DHFR topology reproduces the committed fixture, with the
+    pointer counts of terms."""
+    prm = F.read_amber_prmtop(DHFR / "prmtop")
+    b = F.amber_bonded(prm)
+    d = np.load(GOLDEN / "dhfr_bonded.npz")
+    P = prm["POINTERS"]
+    counts = {"bonds": P["NBONH"] + P["NBONA"], "angles": P["NTHETH"] + P["NTHETA"],
+              "dihedrals": P["NPHIH"] + P["NPHIA"]}
+    for name, (atoms, params) in b.items():
+        assert len(atoms) == counts[name]
+        assert np.array_equal(atoms, d[f"{name}_atoms"])
+        assert np.array_equal(params, d[f"{name}_table"][d[f"{name}_type"]])
+        assert atoms.min() >= 0 and atoms.max() < P["NATOM"]
 
 
 def test_pair_coefficients_from_AB_are_forces():

@@ -90,3 +90,24 @@ def test_bad_arguments():
         oracle.bonded64([[0, 0, 0], [1, 0, 0]], None, ([[0, 2]], [[1.0, 1.0]]))
     with pytest.raises(ValueError):
         oracle.bonded64([[0, 0, 0], [1, 0, 0]], None, ([[-1, 0]], [[1.0, 1.0]]))
+
+
+def test_dhfr_bonded_terms():
+    """The DHFR topology's 36,319 bonded terms on its own coordinates: finite energies of the
+    equilibrated structure, zero net force, and forces equal to minus the energy gradient for a
+    sample of atoms."""
+    from helpers import dhfr_bonded
+    pos, box, T = dhfr_bonded()
+    p64 = pos.astype(np.float64)
+    F, E = oracle.bonded64(p64, box, **T)
+    assert all(np.isfinite(v) and v > 0 for v in E.values())
+    assert np.abs(F.sum(0)).max() <= 1e-9 * np.abs(F).max() * len(F)
+    rng = np.random.default_rng(0)
+    h = 1e-5
+    for i in rng.choice(2489, 8, replace=False):       # protein atoms (all three kinds of terms)
+        for k in range(3):
+            pp, pm = p64.copy(), p64.copy()
+            pp[i, k] += h
+            pm[i, k] -= h
+            num = -(sum(oracle.bonded64(pp, box, **T)[1].values()) - sum(oracle.bonded64(pm, box, **T)[1].values())) / (2 * h)
+            assert abs(F[i, k] - num) <= 1e-4 * max(1.0, abs(F[i, k])), (i, k, F[i, k], num)
