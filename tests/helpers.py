@@ -117,3 +117,66 @@ def dhfr_bonded():
     d = np.load(GOLDEN / "dhfr_bonded.npz")
     terms = {k: (d[f"{k}_atoms"], d[f"{k}_table"][d[f"{k}_type"]]) for k in ("bonds", "angles", "dihedrals")}
     return d["pos"], tuple(float(v) for v in d["box"]), terms
+
+
+def _fma32(a, b, c):
+    """float32 fma emulated through float64 (a*b exact; one rounding of the sum, then to float32:
+    close enough to choose test positions, which the oracle then checks exactly)."""
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+def boundary_dimers(ndimers: int, L: float, rc: float, seed: int, dmin: float = 1.5):
+    """Particles in a periodic cube of edge L, in dimers whose r2 under the reference's rounding
+    (d = fl(xi - xj) with one +-L wrap, r2 = fl(fl(dx^2 + dy^2) + dz^2)) lies exactly on rc2 or
+    one ulp either side of it, and for which r2 computed with a fused multiply-add (fma(dz, dz,
+    dx^2 + dy^2) or fma(dy, dy, dx^2) + dz^2) falls on the other side of the cutoff: a kernel that
+    lets its compiler contract the r2 arithmetic gets these pairs wrong.  No two particles are
+    closer than dmin.  Returns float32 positions (2 ndimers, 3)."""
+    f32 = np.float32
+    rng = np.random.default_rng(seed)
+    Lf, rc2 = f32(L), f32(rc) * f32(rc)
+    h = Lf / f32(2)
+    steps = np.arange(-6, 7)
+    grid = np.stack(np.meshgrid(steps, steps, steps, indexing="ij"), -1).reshape(-1, 3)
+    pts = []
+    tries = 0
+    while len(pts) < 2 * ndimers and tries < 200 * ndimers:
+        tries += 1
+        xi = (rng.random(3) * L).astype(f32)
+        u = rng.standard_normal(3)
+        u /= np.linalg.norm(u)
+        base = np.mod(xi.astype(np.float64) + rc * u, L).astype(f32)
+        # nudge each coordinate of the partner by up to 6 ulps
+        xj = base[None, :].copy().repeat(len(grid), 0)
+        for a in range(3):
+            up = np.nextafter(base[a], f32(np.inf)) - base[a]
+            xj[:, a] = (base[a] + grid[:, a].astype(f32) * up).astype(f32)
+        if (xj < 0).any() or (xj >= Lf).any():
+            continue
+        d = (xi[None, :] - xj).astype(f32)
+        d = np.where(d > h, (d - Lf).astype(f32), np.where(d < -h, (d + Lf).astype(f32), d)).astype(f32)
+        sq = (d * d).astype(f32)
+        ref = ((sq[:, 0] + sq[:, 1]).astype(f32) + sq[:, 2]).astype(f32)
+        fz = _fma32(d[:, 2], d[:, 2], (sq[:, 0] + sq[:, 1]).astype(f32))
+        fy = (_fma32(d[:, 1], d[:, 1], sq[:, 0]) + sq[:, 2]).astype(f32)
+        keep_ref = ref <= rc2
+        flip = (keep_ref != (fz <= rc2)) | (keep_ref != (fy <= rc2))
+        near = np.abs(ref.view(np.int32).astype(np.int64) - int(rc2.view(np.int32))) <= 1
+        cand = np.where(flip & near)[0]
+        if len(cand) == 0:
+            continue
+        pj = xj[rng.choice(cand)]
+        if pts:
+            P = np.asarray(pts, dtype=np.float64)
+            for q in (xi, pj):
+                dd = np.abs(P - q.astype(np.float64))
+                dd = np.minimum(dd, L - dd)
+                if (np.sqrt((dd ** 2).sum(1)) < dmin).any():
+                    break
+            else:
+                pts += [xi, pj]
+        else:
+            pts += [xi, pj]
+    if len(pts) < 2 * ndimers:
+        raise RuntimeError("could not place the dimers")
+    return np.asarray(pts, dtype=f32)

@@ -11,7 +11,7 @@ import pytest
 import oracle
 import sc2019_md_gb300 as m
 from sc2019_md_gb300 import systems
-from helpers import force_err, kat1, kat2_positions, oracle_from_ctx
+from helpers import boundary_dimers, force_err, kat1, kat2_positions, oracle_from_ctx
 
 pytestmark = pytest.mark.gpu
 
@@ -201,6 +201,23 @@ def test_edge_cases():
     assert e.value.status == 3
     with pytest.raises(m.MdrlError):
         m.Context(m.default_params(table_bins=300))
+
+
+@pytest.mark.parametrize("ncell,L,ndimers,seed", [(5, 50.5, 600, 5), (3, 31.5, 300, 6)])
+@pytest.mark.parametrize("tile", [None, (4, 6, 1)])
+def test_cutoff_boundary_pairs(ncell, L, ndimers, seed, tile):
+    """Dimers whose r2 lies exactly on rc2 or one ulp either side under the reference's rounding,
+    chosen so that a fused multiply-add in r2 would decide them the other way (hundreds of such
+    pairs per system): partner counts and the pair total bit-equal to the oracle, with the
+    per-unit shift (5 cells per axis) and the per-pair wrap (3 cells), unpruned and pruned."""
+    pos = boundary_dimers(ndimers, L, 10.0, seed=seed)
+    n = len(pos)
+    rng = np.random.default_rng(seed)
+    q = np.where(rng.permutation(n) < n // 2, -0.42, 0.42).astype(np.float32)
+    sysm = systems.System(name="boundary", box=(L, L, L), cutoff=10.0, ncell=(ncell,) * 3, pos=pos,
+                          vel=np.zeros_like(pos), q=q, type=np.zeros(n, np.int32), sigma=[2.0],
+                          epsilon=[0.1], mass=[39.95], coulomb_k=systems.COULOMB_K)
+    _check_force(sysm, sysm.params(table_bins=512, flags=m.FLAG_ENERGY), tile=tile)
 
 
 @pytest.mark.parametrize("tile", [None, (4, 6, 1), (8, 4, 1)])
