@@ -331,15 +331,20 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     int *wCi = sC + warp * 2 * kChunk;
     int *wCj = wCi + kChunk;
 
-    /* Survivor lists (when the tile asks for pruning): the (32-i tile, 8-j step) pairs of a chunk
-     * whose bounding boxes come within rc.  A lower bound on every pair's r2 from the two boxes decides; the half widths carry a
-     * margin of 2^-20 x the largest box edge, above the rounding of the box centres, widths and
-     * gaps and of the pair differences, so a dropped step holds no pair that passes the filter. */
-    __shared__ float4 s_tb[2][kChunk / 32];
+    /* Survivor lists (when the tile asks for pruning).  The boxes of each group of 4 i-particles
+     * (the 4 rows of one register slot k: i = 32 ti + 4 k + row) are tested against the box of each
+     * 8-j step; a (32-i tile, step) pair survives when any of its 8 groups comes within rc, and
+     * carries the 8-bit mask of those groups, so the step loop skips the dead slots (a
+     * warp-uniform bit test).  A lower bound on every pair's r2 from the two boxes decides; the
+     * half widths carry a margin of 2^-20 x the largest box edge, above the rounding of the box
+     * centres, widths and gaps and of the pair differences, so a dropped slot holds no pair that
+     * passes the filter. */
+    __shared__ float4 s_gb[2][kChunk / 4];
     __shared__ float4 s_sb[2][kChunk / 8];
-    __shared__ unsigned s_mask[(kChunk / 32) * (kChunk / 8) / 32];
+    __shared__ unsigned char s_km[kChunk / 32][kChunk / 8];
     __shared__ int s_nsurv[kChunk / 32];
     __shared__ unsigned char s_list[kChunk / 32][kChunk / 8];
+    __shared__ unsigned char s_klist[kChunk / 32][kChunk / 8];
     const float margin = 9.5367431640625e-07f * fmaxf(g.L[0], fmaxf(g.L[1], g.L[2]));
 
     for (int t = tid; t < ntypes * ntypes; t += (FW * 32)) sCoef[t] = pcoef[t];
@@ -368,7 +373,9 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
             const int nti = (ni + 31) >> 5;
             const int S = (nj + 7) >> 3;                         /* j-steps of 8 */
             if constexpr (PRUNE) {
-            /* boxes: a warp reduces each of its tiles over the 32 lanes; a thread each step */
+            /* boxes: each group of 4 i (4 lanes of a warp, one group per register slot), and a
+             * thread each step.  A group with no particle keeps an empty box (lower > upper), whose
+             * test below fails. */
             for (int ti = warp; ti < nti; ti += FW) {
                 const int il = ti * 32 + lane;
                 float lx = 3.0e38f, ly = 3.0e38f, lz = 3.0e38f, ux = -3.0e38f, uy = -3.0e38f, uz = -3.0e38f;
@@ -377,7 +384,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     lx = ux = pp.x; ly = uy = pp.y; lz = uz = pp.z;
                 }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
+                for (int o = 1; o < 4; o <<= 1) {
                     lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
                     ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
                     lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
@@ -385,13 +392,19 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     uy = fmaxf(uy, __shfl_xor_sync(0xffffffffu, uy, o));
                     uz = fmaxf(uz, __shfl_xor_sync(0xffffffffu, uz, o));
                 }
-                if (lane == 0) {
-                    /* the unit's shift folds into the centre: d = xi - xj + s */
-                    const bool sh = MODE == kDiffShift;
-                    s_tb[0][ti] = make_float4(0.5f * (lx + ux) + (sh ? sx : 0.0f), 0.5f * (ly + uy) + (sh ? sy : 0.0f),
-                                              0.5f * (lz + uz) + (sh ? sz : 0.0f), 0.0f);
-                    s_tb[1][ti] = make_float4(0.5f * (ux - lx) + margin, 0.5f * (uy - ly) + margin,
-                                              0.5f * (uz - lz) + margin, 0.0f);
+                if ((lane & 3) == 0) {
+                    const int gi = ti * 8 + (lane >> 2);
+                    if (lx <= ux) {
+                        /* the unit's shift folds into the centre: d = xi - xj + s */
+                        const bool sh = MODE == kDiffShift;
+                        s_gb[0][gi] = make_float4(0.5f * (lx + ux) + (sh ? sx : 0.0f), 0.5f * (ly + uy) + (sh ? sy : 0.0f),
+                                                  0.5f * (lz + uz) + (sh ? sz : 0.0f), 0.0f);
+                        s_gb[1][gi] = make_float4(0.5f * (ux - lx) + margin, 0.5f * (uy - ly) + margin,
+                                                  0.5f * (uz - lz) + margin, 0.0f);
+                    } else {
+                        s_gb[0][gi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        s_gb[1][gi] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);   /* empty: never kept */
+                    }
                 }
             }
             for (int st = tid; st < S; st += FW * 32) {
@@ -405,14 +418,15 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                 s_sb[1][st] = make_float4(0.5f * (ux - lx), 0.5f * (uy - ly), 0.5f * (uz - lz), 0.0f);
             }
             __syncthreads();
-            /* survivor bit of pair q = ti * S + st (steps before 4 ti are the diagonal's lower half) */
-            for (int q0 = warp * 32; q0 < nti * S; q0 += FW * 32) {
-                const int q = q0 + lane;
-                bool keep = false;
-                if (q < nti * S) {
-                    const int ti = q / S, st = q - ti * S;
-                    if (!diag || st >= 4 * ti) {
-                        const float4 tc = s_tb[0][ti], th = s_tb[1][ti], jc = s_sb[0][st], jh = s_sb[1][st];
+            /* live-group mask of pair q = ti * S + st (steps before 4 ti are the diagonal's lower half) */
+            for (int q = tid; q < nti * S; q += FW * 32) {
+                const int ti = q / S, st = q - ti * S;
+                unsigned km = 0;
+                if (!diag || st >= 4 * ti) {
+                    const float4 jc = s_sb[0][st], jh = s_sb[1][st];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float4 tc = s_gb[0][ti * 8 + k], th = s_gb[1][ti * 8 + k];
                         float ex = tc.x - jc.x, ey = tc.y - jc.y, ez = tc.z - jc.z;
                         if (MODE == kDiffWrap) {
                             ex = wrap_d(ex, g.L[0], g.h[0]); ey = wrap_d(ey, g.L[1], g.h[1]); ez = wrap_d(ez, g.L[2], g.h[2]);
@@ -420,18 +434,17 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                         const float gx = fmaxf(fabsf(ex) - (th.x + jh.x), 0.0f);
                         const float gy = fmaxf(fabsf(ey) - (th.y + jh.y), 0.0f);
                         const float gz = fmaxf(fabsf(ez) - (th.z + jh.z), 0.0f);
-                        keep = gx * gx + gy * gy + gz * gz <= g.rc2;
+                        if (th.x >= 0.0f && gx * gx + gy * gy + gz * gz <= g.rc2) km |= 1u << k;
                     }
                 }
-                const unsigned b = __ballot_sync(0xffffffffu, keep);
-                if (lane == 0) s_mask[q0 >> 5] = b;
+                s_km[ti][st] = (unsigned char)km;
             }
             __syncthreads();
             for (int ti = tid; ti < nti; ti += FW * 32) {
                 int c = 0;
                 for (int st = 0; st < S; ++st) {
-                    const int q = ti * S + st;
-                    if ((s_mask[q >> 5] >> (q & 31)) & 1u) s_list[ti][c++] = (unsigned char)st;
+                    const unsigned char km = s_km[ti][st];
+                    if (km) { s_list[ti][c] = (unsigned char)st; s_klist[ti][c] = km; ++c; }
                 }
                 s_nsurv[ti] = c;
             }
@@ -473,6 +486,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                 int ci[8] = {0, 0, 0, 0, 0, 0, 0, 0};
                 for (int kk = k0; kk < k1; ++kk) {
                     const int jl = (prune ? (int)s_list[ti][kk] : base + kk) * 8 + col;
+                    const unsigned live = prune ? (unsigned)s_klist[ti][kk] : 0xffu;   /* warp-uniform */
                     float xj = -far, yj = -far, zj = -far, qj = 0.0f;
                     int ttj = 0;
                     if (jl < nj) {
@@ -484,6 +498,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     int cj = 0;
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
+                        if (prune && !((live >> k) & 1u)) continue;
                         const float dx = pair_diff<MODE>(xi[k], xj, g.L[0], g.h[0], sx);
                         const float dy = pair_diff<MODE>(yi[k], yj, g.L[1], g.h[1], sy);
                         const float dz = pair_diff<MODE>(zi[k], zj, g.L[2], g.h[2], sz);
