@@ -484,6 +484,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
 #pragma unroll
                 for (int t = 0; t < 24; ++t) fi[t] = 0.0f;
                 int ci[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                bool piece_hit = false;   /* this lane accepted a pair in the piece */
                 for (int kk = k0; kk < k1; ++kk) {
                     const int jl = (prune ? (int)s_list[ti][kk] : base + kk) * 8 + col;
                     const unsigned live = prune ? (unsigned)s_klist[ti][kk] : 0xffu;   /* warp-uniform */
@@ -496,6 +497,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     }
                     float fjx = 0.f, fjy = 0.f, fjz = 0.f;
                     int cj = 0;
+                    bool hit = false;     /* this lane accepted a pair in the step */
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         if (prune && !((live >> k) & 1u)) continue;
@@ -515,6 +517,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                             const float fx = __fmul_rn(fs, dx), fy = __fmul_rn(fs, dy), fz = __fmul_rn(fs, dz);
                             fi[3 * k] += fx; fi[3 * k + 1] += fy; fi[3 * k + 2] += fz;
                             fjx -= fx; fjy -= fy; fjz -= fz;
+                            hit = true;
                             ++acc_pairs;
                             if (EXTRA) {
                                 ++ci[k];
@@ -526,29 +529,37 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                             }
                         }
                     }
+                    /* a step in which no lane accepted a pair adds nothing: without pruning, skip
+                     * its reduction (with pruning nearly every surviving step has a pair, and the
+                     * vote costs more than it saves) */
+                    if (PRUNE || __any_sync(0xffffffffu, hit)) {
+                        piece_hit = piece_hit || hit;
 #pragma unroll
-                    for (int o = 8; o < 32; o <<= 1) {
-                        fjx += __shfl_xor_sync(0xffffffffu, fjx, o);
-                        fjy += __shfl_xor_sync(0xffffffffu, fjy, o);
-                        fjz += __shfl_xor_sync(0xffffffffu, fjz, o);
-                        if (EXTRA) cj += __shfl_xor_sync(0xffffffffu, cj, o);
-                    }
-                    if (row == 0 && jl < nj) {
-                        wFj[jl] += fjx;
-                        wFj[kChunk + jl] += fjy;
-                        wFj[2 * kChunk + jl] += fjz;
-                        if (EXTRA) wCj[jl] += cj;
+                        for (int o = 8; o < 32; o <<= 1) {
+                            fjx += __shfl_xor_sync(0xffffffffu, fjx, o);
+                            fjy += __shfl_xor_sync(0xffffffffu, fjy, o);
+                            fjz += __shfl_xor_sync(0xffffffffu, fjz, o);
+                            if (EXTRA) cj += __shfl_xor_sync(0xffffffffu, cj, o);
+                        }
+                        if (row == 0 && jl < nj) {
+                            wFj[jl] += fjx;
+                            wFj[kChunk + jl] += fjy;
+                            wFj[2 * kChunk + jl] += fjz;
+                            if (EXTRA) wCj[jl] += cj;
+                        }
                     }
                 }
-                reduce_scatter24(fi, col);
-                int cnt_i = 0;
-                if (EXTRA) cnt_i = reduce_scatter8i(ci, col);
-                const int il = ti * 32 + row + 4 * col;
-                if (il < ni) {
-                    wFi[il] += fi[0];
-                    wFi[kChunk + il] += fi[1];
-                    wFi[2 * kChunk + il] += fi[2];
-                    if (EXTRA) wCi[il] += cnt_i;
+                if (PRUNE || __any_sync(0xffffffffu, piece_hit)) {
+                    reduce_scatter24(fi, col);
+                    int cnt_i = 0;
+                    if (EXTRA) cnt_i = reduce_scatter8i(ci, col);
+                    const int il = ti * 32 + row + 4 * col;
+                    if (il < ni) {
+                        wFi[il] += fi[0];
+                        wFi[kChunk + il] += fi[1];
+                        wFi[2 * kChunk + il] += fi[2];
+                        if (EXTRA) wCi[il] += cnt_i;
+                    }
                 }
             }
             __syncthreads();
