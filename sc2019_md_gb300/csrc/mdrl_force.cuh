@@ -365,9 +365,12 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                 sJp[t] = pos[cs + j0 + t];
                 sJt[t] = ptype[cs + j0 + t];
             }
-            for (int t = tid; t < FW * 6 * kChunk; t += (FW * 32)) sF[t] = 0.0f;
+            /* sF and sC start 16-byte aligned (after 16 (2 kChunk + T^2) + 8 kChunk bytes) */
+            for (int t = tid; t < FW * 6 * kChunk / 4; t += (FW * 32))
+                reinterpret_cast<float4 *>(sF)[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (EXTRA)
-                for (int t = tid; t < FW * 2 * kChunk; t += (FW * 32)) sC[t] = 0;
+                for (int t = tid; t < FW * 2 * kChunk / 4; t += (FW * 32))
+                    reinterpret_cast<int4 *>(sC)[t] = make_int4(0, 0, 0, 0);
             __syncthreads();
 
             const int nti = (ni + 31) >> 5;
