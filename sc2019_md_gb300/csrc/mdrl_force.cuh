@@ -5,6 +5,7 @@
  * reference's filter order (SC/Particle_Pair_Gen_HalfShell.v:14-24).  The CTA stages h's and
  * the neighbour's particles (256 at a time) in shared memory.  The (i, j) square is cut into
  * pieces of 32 i-particles x (8 * kStepsPerPiece) j-particles, dealt round-robin to the warps.
+ * Staging uses cp.async: positions (float4) and types go from global to shared memory directly.
  *
  * Inside a piece, lane = row * 8 + col (4 rows x 8 columns): the lane keeps the 8 i-particles
  * i = row + 4k (k < 8) in registers, and in each step takes j = 8 * step + col.  A step
@@ -125,6 +126,20 @@ __device__ __forceinline__ float pair_diff(float a, float b, float L, float h, f
     const float d = __fsub_rn(a, b);
     return MODE == kDiffWrap ? wrap_d(d, L, h) : __fadd_rn(d, s);
 }
+
+/* Asynchronous global -> shared copies (cp.async): a staged particle goes to shared memory
+ * without a round trip through registers, and the copies run while the CTA clears its
+ * accumulators.  cp.async.wait_all is a hardware wait for the thread's own copies (no polling);
+ * the barrier after it makes every thread's copies visible. */
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 /* Sum of v over the 8 column lanes, scattered: on return lane col holds, in v[0..2], the sums of
  * the input v[3*col .. 3*col+2] (each input v has 24 entries). */
@@ -357,13 +372,14 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
             const int ni = min(kChunk, ni_all - i0), nj = min(kChunk, nj_all - j0);
             const bool diag = self && (i0 == j0);
             __syncthreads();
+            /* stage both cells' positions (16 B) and types (4 B) with cp.async */
             for (int t = tid; t < ni; t += (FW * 32)) {
-                sIp[t] = pos[hs + i0 + t];
-                sIt[t] = ptype[hs + i0 + t] * ntypes;
+                cp_async16(sIp + t, pos + hs + i0 + t);
+                cp_async4(sIt + t, ptype + hs + i0 + t);
             }
             for (int t = tid; t < nj; t += (FW * 32)) {
-                sJp[t] = pos[cs + j0 + t];
-                sJt[t] = ptype[cs + j0 + t];
+                cp_async16(sJp + t, pos + cs + j0 + t);
+                cp_async4(sJt + t, ptype + cs + j0 + t);
             }
             /* sF and sC start 16-byte aligned (after 16 (2 kChunk + T^2) + 8 kChunk bytes) */
             for (int t = tid; t < FW * 6 * kChunk / 4; t += (FW * 32))
@@ -371,6 +387,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
             if (EXTRA)
                 for (int t = tid; t < FW * 2 * kChunk / 4; t += (FW * 32))
                     reinterpret_cast<int4 *>(sC)[t] = make_int4(0, 0, 0, 0);
+            cp_async_wait_all();
             __syncthreads();
 
             const int nti = (ni + 31) >> 5;
@@ -478,7 +495,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                         const float4 pp = sIp[il];
                         xi[k] = pp.x; yi[k] = pp.y; zi[k] = pp.z;
                         qi[k] = __fmul_rn(ke, pp.w);
-                        tti[k] = sIt[il];
+                        tti[k] = sIt[il] * ntypes;
                     } else {
                         xi[k] = far; yi[k] = far; zi[k] = far; qi[k] = 0.0f; tti[k] = 0;
                     }
