@@ -263,6 +263,9 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_tot, sizeof(DevTotals));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->h_err, sizeof(unsigned));
+    /* their device addresses, for the kernel that writes them at the end of a force evaluation */
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&c->h_tot_dev, c->h_tot, 0);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&c->h_err_dev, c->h_err, 0);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_mt, 2 * sizeof(MassTab));
     if (e == cudaSuccess) e = cudaMemcpy(c->d_mt, &c->mt_half, sizeof(MassTab), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->d_mt + 1, &c->mt_full, sizeof(MassTab), cudaMemcpyHostToDevice);
@@ -498,9 +501,9 @@ static void *mapped(const mdrl_ctx *c, const void *p) {
     return nullptr;
 }
 
-/* One force evaluation enqueued on the context stream, ending with asynchronous copies of the
- * error word and the totals into pinned host memory; force_eval_finish reads them after the one
- * synchronisation of the call. */
+/* One force evaluation enqueued on the context stream; its last kernel writes the error word and
+ * the totals into pinned host memory (copies when there are no particles); force_eval_finish
+ * reads them after the one synchronisation of the call. */
 static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
                                       const float *q, const int *type, float *fx, float *fy, float *fz,
                                       int *counts, bool stage = false) {
@@ -520,11 +523,13 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
     if (energy) MDRL_TRY(bonded_add_energy(c, n));
     if (n > 0)
         k_unsort_inv<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_inv, c->d_F64, c->d_F32, c->d_cnt, fx, fy,
-                                                          fz, counts);
+                                                          fz, counts, c->d_tot, c->h_tot_dev, c->d_err, c->h_err_dev);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
-    MDRL_CUDA(cudaMemcpyAsync(c->h_tot, c->d_tot, sizeof(DevTotals), cudaMemcpyDeviceToHost, c->stream));
-    MDRL_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    if (n == 0) {
+        MDRL_CUDA(cudaMemcpyAsync(c->h_tot, c->d_tot, sizeof(DevTotals), cudaMemcpyDeviceToHost, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    }
     c->have_state = false; /* the sorted buffers now hold this evaluation */
     return MDRL_OK;
 }

@@ -97,6 +97,8 @@ struct mdrl_ctx {
     DevTotals *d_tot = nullptr;
     DevTotals *h_tot = nullptr;  /* pinned host copies, read back with the results of a call */
     unsigned *h_err = nullptr;
+    DevTotals *h_tot_dev = nullptr;  /* the same two, as device addresses */
+    unsigned *h_err_dev = nullptr;
     unsigned *d_err = nullptr;
     int num_sms = 0;
 

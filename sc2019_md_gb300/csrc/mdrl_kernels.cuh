@@ -424,8 +424,13 @@ static __global__ void k_unsort(int n, const int *__restrict__ pid, const unsign
 static __global__ void k_unsort_inv(int n, const int *__restrict__ inv, const unsigned long long *__restrict__ F64,
                                     const float *__restrict__ F32, const int *__restrict__ cnt_s,
                                     float *__restrict__ fx, float *__restrict__ fy, float *__restrict__ fz,
-                                    int *__restrict__ cnt_u) {
+                                    int *__restrict__ cnt_u, const DevTotals *__restrict__ tot_d = nullptr,
+                                    DevTotals *tot_h = nullptr, const unsigned *__restrict__ err_d = nullptr,
+                                    unsigned *err_h = nullptr) {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    /* the call's last kernel also hands the totals and the error word to pinned (mapped) host
+     * memory: both are final here (stream order), and the call needs no copies after it */
+    if (id == 0 && tot_h) { *tot_h = *tot_d; *err_h = *err_d; }
     if (id >= n) return;
     const int k = inv[id];
     if (F64) {
