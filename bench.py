@@ -241,9 +241,9 @@ def run_ours(args, rank, world, local, dist):
         fms.append(ctx.time_force())
     ctx.close()
 
-    # ---- optional: the same step with smooth-PME long-range electrostatics -----------------
+    # ---- the same step with smooth-PME long-range electrostatics (charged systems) -----------
     pme_out = None
-    if args.pme:
+    if not args.no_pme and sysm.q is not None:
         ctxl = m.Context(params)
         pme_p = ctxl.set_pme(order=args.pme_order)
         ctxl.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
@@ -599,7 +599,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile (no autotuning)")
     ap.add_argument("--tile", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
                     help="fixed tile warps,steps,prune instead of autotuning (e.g. 4,6,1)")
-    ap.add_argument("--pme", action="store_true", help="also time the step with smooth-PME electrostatics")
+    ap.add_argument("--no-pme", action="store_true", help="skip timing the step with smooth-PME electrostatics")
     ap.add_argument("--pme-order", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
