@@ -37,7 +37,7 @@ using namespace mdrl;
 
 namespace mdrl {
 
-constexpr double kPmeFix = 1099511627776.0;          /* 2^40 grid units per e */
+constexpr float kPmeFix = 1099511627776.0f;          /* 2^40 grid units per e */
 constexpr float kPmeFixInv = 9.094947017729282e-13f; /* 2^-40 */
 constexpr int kPmeEnergyBlocks = 256;
 
@@ -126,8 +126,11 @@ __global__ void k_pme_spread(int n, const float4 *__restrict__ pos, PmeGeom pg,
 #pragma unroll
                     for (int j2 = 0; j2 < P; ++j2) {
                         const float v = q1 * th[2][j2];
+                        /* v 2^40 is exact in FP32 (a power-of-two scale), so rounding it to an
+                         * integer gives the same value as the same product in FP64 would, without
+                         * FP64 arithmetic (slow on this part) */
                         atomicAdd(qfix + g1 + wrapk(k0[2] - j2, pg.K[2]),
-                                  (unsigned long long)__double2ll_rn((double)v * kPmeFix));
+                                  (unsigned long long)__float2ll_rn(v * kPmeFix));
                     }
                 }
             }
