@@ -357,13 +357,13 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
 /* ---- kernel dispatch ---------------------------------------------------------------------- */
 
 namespace mdrl {
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw, bool prune) {
-    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false>(order, sep, extra, wrap);
-    if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false>(order, sep, extra, wrap);
-    if (fw == 8) return prune ? pick_force_set<0, 8, true>(order, sep, extra, wrap)
-                              : pick_force_set<0, 8, false>(order, sep, extra, wrap);
-    return prune ? pick_force_set<0, 4, true>(order, sep, extra, wrap)
-                 : pick_force_set<0, 4, false>(order, sep, extra, wrap);
+force_fn pick_force(int order, bool sep, bool extra, int acc, int fw, bool prune) {
+    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false>(order, sep, extra);
+    if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false>(order, sep, extra);
+    if (fw == 8) return prune ? pick_force_set<0, 8, true>(order, sep, extra)
+                              : pick_force_set<0, 8, false>(order, sep, extra);
+    return prune ? pick_force_set<0, 4, true>(order, sep, extra)
+                 : pick_force_set<0, 4, false>(order, sep, extra);
 }
 
 force_fn pick_force_batch(int order, bool sep, bool extra, bool prune) {
@@ -389,11 +389,9 @@ int mdrl::eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 
 
 static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra,
                                      unsigned long long *F64, float *F32) {
-    /* the per-unit shift needs >= 4 cells on every axis; with 3 the per-pair wrap is used */
-    const bool wrap = c->g.nc[0] < 4 || c->g.nc[1] < 4 || c->g.nc[2] < 4;
     const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
     const bool prune = c->p.accum == MDRL_ACC_FIXED64 && c->tile.prune_steps;
-    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, wrap, fw, prune);
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, fw, prune);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const int units = c->ncells * kHalfShellCells;

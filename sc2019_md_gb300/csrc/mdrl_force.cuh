@@ -17,12 +17,15 @@
  * one atomic per particle and component (int64 fixed point 2^-24: exact, so the result does not
  * depend on the order in which CTAs finish).
  *
- * Periodic wrap.  With at least 4 cells of edge >= rc on every axis, whether the reference's
- * one-wrap rule (d > L/2 -> d - L, d < -L/2 -> d + L; SC/r2_compute_with_pbc.v:81-127) fires
- * for a pair depends only on whether the neighbour cell lies across the box boundary, so the
- * unit adds a precomputed -L, 0 or +L to fl(xi - xj): the same two roundings as the per-pair
- * rule, hence the same r2 bit for bit.  With 3 cells on an axis the per-pair rule is kept
- * (WRAP = true).
+ * Periodic wrap.  The reference applies one wrap per pair (d > L/2 -> d - L, d < -L/2 -> d + L;
+ * SC/r2_compute_with_pbc.v:81-127).  A unit instead adds a precomputed -L, 0 or +L to
+ * fl(xi - xj) per axis, by whether the neighbour cell lies across the box boundary: the same two
+ * roundings.  With at least 3 cells of edge e >= rc per axis (L = n e) the two rules agree on
+ * every pair that can pass the filter: where they differ, the unit's rule leaves |d| above 1.5 e
+ * or the reference's leaves it above e (adjacent cells are less than 2 e apart, cells across the
+ * boundary more than e), both above rc; so the accepted pairs and their d are bit-identical
+ * (checked exhaustively on 3-cell systems with particles on cell and box faces).  WRAP = true
+ * keeps the per-pair rule for explicit cell pairs of small boxes (batches).
  *
  * Within a cell the particles are in Morton order of their position inside the cell, so the 4 i
  * x 8 j candidates of one warp instruction are spatially coherent: for ~70 % of them no lane
@@ -69,7 +72,7 @@ typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDe
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
 
 /* fw: warps per CTA (8 only with int64 fixed point); prune: survivor lists (fixed point only) */
-force_fn pick_force(int order, bool sep, bool extra, int acc, bool wrap, int fw = kFW, bool prune = false);
+force_fn pick_force(int order, bool sep, bool extra, int acc, int fw = kFW, bool prune = false);
 /* the batched-replica instantiation (int64 fixed point, difference rule per item) */
 force_fn pick_force_batch(int order, bool sep, bool extra, bool prune);
 
@@ -116,9 +119,9 @@ __device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2,
 }
 
 /* Pair difference rules of a unit (both give the reference's d for every pair that can pass the
- * filter; see k_force):
- *   kDiffShift  fl(fl(xi - xj) + s)        (the unit's -L/0/+L shift, >= 4 cells per axis)
- *   kDiffWrap   the one-wrap rule per pair (3-cell grids, cell pairs of small boxes) */
+ * filter; see the header):
+ *   kDiffShift  fl(fl(xi - xj) + s)        (the unit's -L/0/+L shift: half-shell units)
+ *   kDiffWrap   the one-wrap rule per pair (explicit cell pairs of small boxes in batches) */
 enum : int { kDiffShift = 1, kDiffWrap = 2 };
 
 template <int MODE>
@@ -708,8 +711,9 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         unit = it.unit;
         coff = rp.cell_off;
         cell_pair = rp.path == kPathMinImage;
-        /* the per-unit shift needs >= 4 cells per axis; 3-cell grids and cell pairs wrap per pair */
-        use_wrap = cell_pair || gb.nc[0] < 4 || gb.nc[1] < 4 || gb.nc[2] < 4;
+        /* half-shell items take the per-unit shift (exact for every pair that can pass the
+         * filter, see the header); explicit cell pairs wrap per pair */
+        use_wrap = cell_pair;
     }
     const Geom &g = BATCH ? gb : gparam;
     int h, c;
@@ -754,12 +758,11 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
  * Each set is instantiated explicitly in one translation unit (mdrl_force_*.cu), so the sets
  * compile in parallel; everywhere else the declarations below keep them from being instantiated. */
 template <int ACC, int FW, bool PRUNE>
-force_fn pick_force_set(int order, bool sep, bool extra, bool wrap) {
+force_fn pick_force_set(int order, bool sep, bool extra) {
     auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return wrap ? (force_fn)k_force<O, S, E, ACC, true, false, FW, PRUNE>
-                    : (force_fn)k_force<O, S, E, ACC, false, false, FW, PRUNE>;
+        return (force_fn)k_force<O, S, E, ACC, false, false, FW, PRUNE>;
     };
     auto se = [&](auto ord) -> force_fn {
         using T = std::true_type;
@@ -796,12 +799,12 @@ force_fn pick_batch_set(int order, bool sep, bool extra) {
     }
 }
 
-extern template force_fn pick_force_set<0, 4, false>(int, bool, bool, bool);
-extern template force_fn pick_force_set<0, 4, true>(int, bool, bool, bool);
-extern template force_fn pick_force_set<0, 8, false>(int, bool, bool, bool);
-extern template force_fn pick_force_set<0, 8, true>(int, bool, bool, bool);
-extern template force_fn pick_force_set<1, 4, false>(int, bool, bool, bool);
-extern template force_fn pick_force_set<2, 4, false>(int, bool, bool, bool);
+extern template force_fn pick_force_set<0, 4, false>(int, bool, bool);
+extern template force_fn pick_force_set<0, 4, true>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, false>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, true>(int, bool, bool);
+extern template force_fn pick_force_set<1, 4, false>(int, bool, bool);
+extern template force_fn pick_force_set<2, 4, false>(int, bool, bool);
 extern template force_fn pick_batch_set<false>(int, bool, bool);
 extern template force_fn pick_batch_set<true>(int, bool, bool);
 

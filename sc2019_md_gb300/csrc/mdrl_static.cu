@@ -261,9 +261,8 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
         k_gather_user<<<grid, blk, 0, st>>>(n, d_sorted, x, y, z, q, type, d_pos, d_type, d_id, d_F64, nullptr,
                                             nullptr, p->ntypes, d_err);
     }
-    const bool wrap = g.nc[0] < 4 || g.nc[1] < 4 || g.nc[2] < 4;
     const int ord = p->eval == MDRL_EVAL_DIRECT ? 0 : order;
-    force_fn fn = pick_force(ord, p->arith == MDRL_ARITH_SEPARATE, false, MDRL_ACC_FIXED64, wrap);
+    force_fn fn = pick_force(ord, p->arith == MDRL_ARITH_SEPARATE, false, MDRL_ACC_FIXED64);
     const size_t smem = force_smem_bytes(p->ntypes, false);
     ST_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)force_smem_bytes(MDRL_MAX_TYPES, true, 8)));
