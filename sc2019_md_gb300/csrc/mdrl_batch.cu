@@ -10,8 +10,8 @@
  * one force launch over a work list, second kick, totals.
  *
  * Force work list.  A replica with at least 3 cells of edge >= rc per axis contributes its
- * ncells x 14 half-shell units (the single-system kernel, per-pair wrap, the replica's geometry
- * and cell offset).  One with fewer cells but every edge above 2 rc contributes every pair of its
+ * ncells x 14 half-shell units (the single-system kernel with its per-unit periodic shift, the
+ * replica's geometry and cell offset).  One with fewer cells but every edge above 2 rc contributes every pair of its
  * cells (a <= b) within reach, evaluated by the same tiled Newton-3 code with the per-pair
  * minimum image.  One with an edge of at most 2 rc (always above rc) contributes blocks of 128
  * particles that sum every periodic image within rc.  Items are ordered by estimated cost,

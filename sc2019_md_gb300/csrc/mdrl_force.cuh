@@ -219,7 +219,7 @@ __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32,
 /* ---- batched replicas ----------------------------------------------------------------------
  * One launch covers every replica of a batch; a work item is one of
  *   (replica, half-shell unit)  at least 3 cells of edge >= rc per axis: the path below with the
- *                               replica's geometry and cell offset (per-pair wrap);
+ *                               replica's geometry and cell offset (per-unit shift);
  *   (replica, cell pair a <= b) every edge above 2 rc but fewer cells: the same tiled Newton-3
  *                               path over an explicit pair of cells, per-pair minimum image;
  *   (replica, 128 particles)    an edge of at most 2 rc (always above rc): every periodic image
