@@ -77,6 +77,14 @@ enum {
 #define MDRL_FLAG_ENERGY 0x1u      /* evaluate LJ / Coulomb energy and the virial every step */
 #define MDRL_FLAG_PAIR_COUNTS 0x2u /* count partners per particle (pair-list parity) */
 #define MDRL_FLAG_NO_PBC 0x4u      /* no periodic wrap of pair differences (mdrl_pair_eval) */
+/* Pair differences as the exact minimum-image difference rounded once: the box edge is taken off
+ * the coordinate on the far (high) side first, which is exact, so a pair across the boundary
+ * keeps FP32 relative precision in d.  Without the flag the reference's datapath is used,
+ * d = fl(fl(xi - xj) -+ L) (SC/r2_compute_with_pbc.v:81-127; MD_Evaluation_Model.cpp:77-99),
+ * whose first rounding is an absolute error up to ulp(L)/2; its pair list is the reference's
+ * bit for bit.  The two rules give the same pair set except for pairs within a few ulps of rc.
+ * Fused arithmetic (MDRL_ARITH_FMA) only; single-system contexts and mdrl_force_eval_static. */
+#define MDRL_FLAG_EXACT_DIFF 0x8u
 
 typedef struct {
     double box[3];         /* periodic box edges, Angstrom; positions live in [0, box) */
@@ -145,6 +153,17 @@ void mdrl_default_params(mdrl_params *p);
  * equally spaced points (the reference uses 8). */
 mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples, float *coef);
 
+/* Table polynomial forms (mdrl_set_tables' flags, mdrl_get_table_form). */
+#define MDRL_TABLE_RAW 0x1        /* the coefficients carry their physical prefactors */
+#define MDRL_TABLE_BIN_LOCAL 0x2  /* plane k holds the coefficient of u^k, u = r2 - (start of r2's
+                                     bin); orders 2-3.  u is exact in FP32, so the polynomial has
+                                     no cancellation between large monomial terms.  The library
+                                     fits its own order-2 and order-3 tables in this form. */
+
+/* The same fit in the bin-local form (MDRL_TABLE_BIN_LOCAL): plane k holds the coefficient of
+ * u^k.  No counterpart in the reference, whose tables are monomial in r2. */
+mdrl_status mdrl_fit_tables_bin_local(int order, int nseg, int bins, int min_log2, int samples, float *coef);
+
 /* Create / destroy a context.  Validates the parameters, builds the FP64-fitted tables and
  * uploads them; device buffers for particles are sized on first use. */
 mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out);
@@ -152,14 +171,19 @@ mdrl_status mdrl_destroy(mdrl_ctx *ctx);
 
 /* Replace the generated tables, e.g. with the reference's ROM images.  coef holds nfunc
  * functions (2: r^-14, r^-8; 3: + r^-3; 6: + r^-12, r^-6, r^-1), each as (order+1) planes of
- * nseg*bins coefficients, plane k holding the coefficient of r2^k.  When raw_coefficients is
- * nonzero the tables already carry their physical prefactors (as the reference's do) and the
- * per-type multipliers become A = 1, B = -1, ke*qi*qj unchanged. */
+ * nseg*bins coefficients, plane k holding the coefficient of r2^k.  flags (MDRL_TABLE_*):
+ * MDRL_TABLE_RAW (the value 1 of the earlier raw_coefficients argument) when the tables already
+ * carry their physical prefactors (as the reference's do) -- the per-type multipliers become
+ * A = 1, B = -1, ke*qi*qj unchanged; MDRL_TABLE_BIN_LOCAL when the planes are coefficients of
+ * u = r2 - bin start (orders 2-3 only). */
 mdrl_status mdrl_set_tables(mdrl_ctx *ctx, int order, int nseg, int bins, int min_log2, int nfunc,
-                            const float *coef, int raw_coefficients);
+                            const float *coef, int flags);
 
-/* Read back the tables in use (same layout as mdrl_set_tables with nfunc = 6).  Pass coef = NULL
- * to query the sizes. */
+/* The MDRL_TABLE_* flags of the tables in use. */
+mdrl_status mdrl_get_table_form(mdrl_ctx *ctx, int *flags);
+
+/* Read back the tables in use (same layout as mdrl_set_tables with nfunc = 6; the form from
+ * mdrl_get_table_form).  Pass coef = NULL to query the sizes. */
 mdrl_status mdrl_get_tables(mdrl_ctx *ctx, int *order, int *nseg, int *bins, int *min_log2,
                             float *coef);
 
@@ -249,9 +273,12 @@ mdrl_status mdrl_time_force(mdrl_ctx *ctx, float *ms);
  * (q and type may be NULL); stream is a cudaStream_t (NULL = the legacy default stream); the
  * call synchronises that stream.  *pairs_out (optional) receives the number of pairs.
  * Limits: n <= 131072, <= 4096 cells, nseg * bins <= 16384, MDRL_ACC_FIXED64 only; beyond them
- * the call returns MDRL_ERR_RANGE.  The first call on a device looks up the array's device
- * address (make it before any stream capture).  All calls share the array and it keeps the last
- * call's contents: calls whose GPU work overlaps race and must be serialised by the caller. */
+ * the call returns MDRL_ERR_RANGE.  The call runs on the current device, which must be
+ * p->device (else MDRL_ERR_INVALID_ARG).  Every call looks up the array's address in the current
+ * CUDA context; the first call in a context (and any call whose table parameters differ from the
+ * previous call's) copies the tables in with synchronous host copies, so make it before any stream
+ * capture.  All calls share the array and it keeps the last call's contents: calls whose GPU work
+ * overlaps race and must be serialised by the caller. */
 mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const float *x, const float *y,
                                    const float *z, const float *q, const int *type, float *fx,
                                    float *fy, float *fz, int64_t *pairs_out, void *stream);

@@ -23,7 +23,7 @@ class OrcSys(C.Structure):
         ("box", C.c_float * 3), ("ncell", C.c_int * 3), ("rc2", C.c_float), ("ntypes", C.c_int),
         ("pcoef", _F), ("ke", C.c_float), ("eval", C.c_int), ("arith", C.c_int),
         ("order", C.c_int), ("nseg", C.c_int), ("bins", C.c_int), ("min_log2", C.c_int),
-        ("tab", _F), ("pcoef64", _D), ("ke64", C.c_double),
+        ("tab", _F), ("pcoef64", _D), ("ke64", C.c_double), ("local", C.c_int), ("exact", C.c_int),
     ]
 
 
@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
         L.orc_force_cells.argtypes = [C.POINTER(OrcSys), _D, _D, _I, C.POINTER(OrcStats)]
         L.orc_force_direct64.argtypes = [C.POINTER(OrcSys), _D, C.POINTER(OrcStats)]
         L.orc_force_tables64.argtypes = [C.POINTER(OrcSys), _D, C.POINTER(OrcStats)]
+        L.orc_force_split64.argtypes = [C.POINTER(OrcSys), C.c_int, C.c_int, _D, C.POINTER(OrcStats)]
         L.orc_force_cells_mt.argtypes = [C.POINTER(OrcSys), C.c_int, C.c_int, C.c_int, _F]
         L.orc_force_cells_mt.restype = C.c_int64
         L.orc_force_allpairs_mt.argtypes = [C.POINTER(OrcSys), C.c_int, _F]
@@ -75,7 +76,8 @@ class System:
     """Arrays + parameters of one system, kept alive for the C structure that points at them."""
 
     def __init__(self, pos, box, ncell, cutoff, pcoef, q=None, type=None, ke=0.0, tab=None,
-                 order=1, nseg=0, bins=256, min_log2=-2, eval=0, arith=0, pcoef64=None, ke64=0.0):
+                 order=1, nseg=0, bins=256, min_log2=-2, eval=0, arith=0, pcoef64=None, ke64=0.0,
+                 local=False, exact=False):
         pos = np.asarray(pos, np.float32)
         self.x = np.ascontiguousarray(pos[:, 0])
         self.y = np.ascontiguousarray(pos[:, 1])
@@ -103,6 +105,8 @@ class System:
         s.tab = _p(self.tab, _F)
         s.pcoef64 = _p(self.pcoef64, _D)
         s.ke64 = ke64
+        s.local = int(bool(local))
+        s.exact = int(bool(exact))
         self.s = s
         self.n = n
 
@@ -122,6 +126,13 @@ class System:
     def force_tables64(self):
         F = np.zeros((self.n, 3)); st = OrcStats()
         assert lib().orc_force_tables64(C.byref(self.s), _p(F, _D), C.byref(st)) >= 0
+        return F, st.as_dict()
+
+    def force_split64(self, f32_diff: bool, tables: bool):
+        """FP64 forces on the accepted pairs with the datapath's rounded differences or exact
+        ones, and tables (evaluated in FP64) or direct powers: the error decomposition."""
+        F = np.zeros((self.n, 3)); st = OrcStats()
+        assert lib().orc_force_split64(C.byref(self.s), int(f32_diff), int(tables), _p(F, _D), C.byref(st)) >= 0
         return F, st.as_dict()
 
     def force_cells_mt(self, nthreads=0, hbegin=0, hend=-1):
@@ -191,12 +202,13 @@ def read_pdb_like_reference(path, n):
     return np.asarray([[np.float32(v) for v in l.split()[6:9]] for l in lines], np.float32)
 
 
-def fit_tables(order, nseg, bins, min_log2, samples=8):
+def fit_tables(order, nseg, bins, min_log2, samples=8, local=False):
     """Independent numpy restatement of the table fit of
     MatlabScripts/LJ_no_smooth_poly_interpolation_function.m:182-378: per power-of-two segment and
     bin, a least-squares polynomial through `samples` points x_i = bin_start + i*width/samples of
     the unit functions x^-7, x^-4, x^-1.5, x^-6, x^-3, x^-0.5 (x = r2).  FP64 normal-equation fit
-    in the bin-local variable, returned as FP32 monomial coefficients (6, order+1, nseg*bins)."""
+    in the bin-local variable, returned as FP32 monomial coefficients (6, order+1, nseg*bins), or
+    with local=True as coefficients of u = r2 - bin start (the library's order-2/3 form)."""
     expo = np.array([-7.0, -4.0, -1.5, -6.0, -3.0, -0.5])
     seg = np.repeat(np.arange(nseg), bins)
     b = np.tile(np.arange(bins), nseg)
@@ -211,6 +223,9 @@ def fit_tables(order, nseg, bins, min_log2, samples=8):
     for f, e in enumerate(expo):
         y = (x0[:, None] + t[None, :] * w[:, None]) ** e     # (nidx, samples)
         a = y @ pinv.T                                       # (nidx, order+1) in t
+        if local:
+            out[f] = (a / w[:, None] ** np.arange(order + 1)[None, :]).T.astype(np.float32)
+            continue
         c = np.zeros_like(a)
         for mm in range(order + 1):
             am = a[:, mm] / w ** mm

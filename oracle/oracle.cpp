@@ -45,14 +45,23 @@ inline float wrap1(float d, float L, int *dir) {
 inline float mul(float a, float b) { return a * b; }
 inline float add(float a, float b) { return a + b; }
 
-/* Polynomial c_order*r2^order + ... + c0 by Horner's rule, one coefficient plane per power. */
+/* Start of table bin idx: 2^(min_log2 + seg) * (1 + bin / bins), exact in FP32 and FP64. */
+inline double bin_start(const orc_sys *s, int idx) {
+    const int seg = idx / s->bins, bin = idx - seg * s->bins;
+    return ldexp(1.0 + (double)bin / s->bins, s->min_log2 + seg);
+}
+
+/* Polynomial c_order*x^order + ... + c0 by Horner's rule, one coefficient plane per power;
+ * x = r2 (monomial tables) or u = r2 - bin start (bin-local tables; exact in FP32, r2 lying in
+ * the bin). */
 inline float poly32(const orc_sys *s, int f, int idx, float r2) {
     const int nidx = s->nseg * s->bins;
     const float *t = s->tab + (size_t)f * (s->order + 1) * nidx;
+    const float x = s->local ? r2 - (float)bin_start(s, idx) : r2;
     float v = t[(size_t)s->order * nidx + idx];
     for (int k = s->order - 1; k >= 0; --k) {
         const float c = t[(size_t)k * nidx + idx];
-        v = s->arith ? add(mul(v, r2), c) : fmaf(v, r2, c);
+        v = s->arith ? add(mul(v, x), c) : fmaf(v, x, c);
     }
     return v;
 }
@@ -60,8 +69,9 @@ inline float poly32(const orc_sys *s, int f, int idx, float r2) {
 inline double poly64(const orc_sys *s, int f, int idx, double r2) {
     const int nidx = s->nseg * s->bins;
     const float *t = s->tab + (size_t)f * (s->order + 1) * nidx;
+    const double x = s->local ? r2 - bin_start(s, idx) : r2;
     double v = t[(size_t)s->order * nidx + idx];
-    for (int k = s->order - 1; k >= 0; --k) v = v * r2 + (double)t[(size_t)k * nidx + idx];
+    for (int k = s->order - 1; k >= 0; --k) v = v * x + (double)t[(size_t)k * nidx + idx];
     return v;
 }
 
@@ -95,11 +105,27 @@ struct PairOut { float fx, fy, fz, fs, r2, elj, ec; int below; int dir[3]; float
  * In fused mode each "x*y + z" above is one fmaf. */
 inline int pair32_at(const orc_sys *s, float qi, int ti, float qj, int tj, PairOut *o);
 
+/* The exact-difference rule: the wrap direction as wrap1 decides it, then the box edge comes off
+ * the high coordinate (xi - L when xi is the high one, xj - L otherwise; exact for coordinates in
+ * [0, L)) and the difference is rounded once. */
+inline float wrap_exact(float xi, float xj, float L, int *dir) {
+    float d = wrap1(xi - xj, L, dir);
+    if (*dir < 0) d = (xi - L) - xj;
+    else if (*dir > 0) d = xi - (xj - L);
+    return d;
+}
+
 inline int pair32(const orc_sys *s, float xi, float yi, float zi, float qi, int ti, float xj,
                   float yj, float zj, float qj, int tj, PairOut *o) {
-    o->dx = wrap1(xi - xj, s->box[0], &o->dir[0]);
-    o->dy = wrap1(yi - yj, s->box[1], &o->dir[1]);
-    o->dz = wrap1(zi - zj, s->box[2], &o->dir[2]);
+    if (s->exact) {
+        o->dx = wrap_exact(xi, xj, s->box[0], &o->dir[0]);
+        o->dy = wrap_exact(yi, yj, s->box[1], &o->dir[1]);
+        o->dz = wrap_exact(zi, zj, s->box[2], &o->dir[2]);
+    } else {
+        o->dx = wrap1(xi - xj, s->box[0], &o->dir[0]);
+        o->dy = wrap1(yi - yj, s->box[1], &o->dir[1]);
+        o->dz = wrap1(zi - zj, s->box[2], &o->dir[2]);
+    }
     return pair32_at(s, qi, ti, qj, tj, o);
 }
 
@@ -316,6 +342,55 @@ int orc_force_direct64(const orc_sys *s, double *F, orc_stats *st) {
         acc.e_lj += pc[3] * i6 + pc[2] * i12;
         acc.e_coul += qq * i1;
         acc.virial += fs * r2;
+        F[3 * i] += fs * dx; F[3 * i + 1] += fs * dy; F[3 * i + 2] += fs * dz;
+        F[3 * j] -= fs * dx; F[3 * j + 1] -= fs * dy; F[3 * j + 2] -= fs * dz;
+    });
+    if (st) *st = acc;
+    return c.maxocc;
+}
+
+int orc_force_split64(const orc_sys *s, int f32_diff, int tables, double *F, orc_stats *st) {
+    if (check_sys(s) || !s->pcoef64 || (tables && s->eval != 0)) return -1;
+    Cells c;
+    build_cells(s, &c);
+    const int n = s->n;
+    memset(F, 0, sizeof(double) * 3 * n);
+    orc_stats acc;
+    memset(&acc, 0, sizeof(acc));
+    const int ncells = c.nc[0] * c.nc[1] * c.nc[2];
+    for_each_candidate(s, c, 0, ncells, [&](int i, int j) {
+        PairOut o;
+        acc.candidates++;
+        if (!pair32(s, s->x[i], s->y[i], s->z[i], qof(s, i), s->type[i], s->x[j], s->y[j],
+                    s->z[j], qof(s, j), s->type[j], &o))
+            return;
+        acc.pairs++;
+        double dx, dy, dz;
+        if (f32_diff == 1) {
+            dx = o.dx; dy = o.dy; dz = o.dz;   /* the datapath's rounded fl(fl(xi - xj) +- L) */
+        } else {
+            dx = (double)s->x[i] - (double)s->x[j] + o.dir[0] * (double)s->box[0];
+            dy = (double)s->y[i] - (double)s->y[j] + o.dir[1] * (double)s->box[1];
+            dz = (double)s->z[i] - (double)s->z[j] + o.dir[2] * (double)s->box[2];
+            if (f32_diff == 2) {   /* the exact minimum-image difference rounded once */
+                dx = (float)dx; dy = (float)dy; dz = (float)dz;
+            }
+        }
+        double r2 = dx * dx + dy * dy + dz * dz;
+        const double *pc = s->pcoef64 + 4 * (s->type[i] * s->ntypes + s->type[j]);
+        const double qq = s->ke64 * (double)qof(s, i) * (double)qof(s, j);
+        double fs;
+        if (tables) {
+            float r2e;
+            int below;
+            const int idx = table_index(s, o.r2, &r2e, &below);
+            if (below) r2 = r2e;
+            fs = pc[1] * poly64(s, ORC_F8, idx, r2) + pc[0] * poly64(s, ORC_F14, idx, r2);
+            if (s->ke != 0.0f) fs += qq * poly64(s, ORC_F3, idx, r2);
+        } else {
+            const double i2 = 1.0 / r2, i4 = i2 * i2, i8 = i4 * i4, i14 = i8 * i4 * i2;
+            fs = (qq * i2 * sqrt(i2) + pc[1] * i8) + pc[0] * i14;
+        }
         F[3 * i] += fs * dx; F[3 * i + 1] += fs * dy; F[3 * i + 2] += fs * dz;
         F[3 * j] -= fs * dx; F[3 * j + 1] -= fs * dy; F[3 * j + 2] -= fs * dz;
     });

@@ -59,6 +59,9 @@ typedef struct {
     const float *tab;    /* [ORC_NFUNC][order+1][nseg*bins] */
     const double *pcoef64; /* [ntypes*ntypes*4] FP64 mixing coefficients for orc_force_direct64 */
     double ke64;
+    int local;           /* tables: 0 monomial in r2, 1 coefficients of u = r2 - bin start */
+    int exact;           /* differences: 0 the reference's fl(fl(xi - xj) -+ L), 1 the exact
+                            minimum-image difference rounded once (edge off the high coordinate) */
 } orc_sys;
 
 typedef struct {
@@ -91,6 +94,12 @@ int orc_force_direct64(const orc_sys *s, double *F, orc_stats *st);
 
 /* Same pair set, FP64 evaluation of the FP32 table polynomials (index from the FP32 r2). */
 int orc_force_tables64(const orc_sys *s, double *F, orc_stats *st);
+
+/* The pieces of the force error, for its decomposition: the same accepted pairs with FP64
+ * arithmetic throughout, the differences exact (f32_diff = 0) or the FP32 datapath's rounded
+ * d = fl(fl(xi - xj) +- L) (f32_diff = 1), and the pair functions as direct FP64 powers
+ * (tables = 0) or the FP32 tables evaluated in FP64 (tables = 1, as orc_force_tables64). */
+int orc_force_split64(const orc_sys *s, int f32_diff, int tables, double *F, orc_stats *st);
 
 /* Multi-threaded FP32 half-shell force (the timed CPU baseline) over home cells
  * [hbegin, hend) (hend < 0: all).  F[3n] float.  Returns the number of pairs evaluated. */

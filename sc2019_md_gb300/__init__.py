@@ -18,7 +18,8 @@ __all__ = [
     "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PmeParams", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
     "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
-    "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "MAX_TYPES", "STATUS",
+    "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "FLAG_EXACT_DIFF", "TABLE_RAW",
+    "TABLE_BIN_LOCAL", "MAX_TYPES", "STATUS",
 ]
 
 MAX_TYPES = 16
@@ -26,7 +27,8 @@ ACC_FIXED64, ACC_FP32_ATOMIC, ACC_KAHAN = 0, 1, 2
 ARITH_FMA, ARITH_SEPARATE = 0, 1
 EVAL_TABLE, EVAL_DIRECT = 0, 1
 INT_VELOCITY_VERLET, INT_EULER = 0, 1
-FLAG_ENERGY, FLAG_PAIR_COUNTS, FLAG_NO_PBC = 0x1, 0x2, 0x4
+FLAG_ENERGY, FLAG_PAIR_COUNTS, FLAG_NO_PBC, FLAG_EXACT_DIFF = 0x1, 0x2, 0x4, 0x8
+TABLE_RAW, TABLE_BIN_LOCAL = 0x1, 0x2
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CELL_OVERFLOW", 3: "RANGE", 4: "CUDA_ERROR",
           5: "TIMEOUT", 6: "STATE"}
 
@@ -120,6 +122,8 @@ def lib() -> C.CDLL:
     L.mdrl_default_params.argtypes = [C.POINTER(Params)]
     L.mdrl_default_params.restype = None
     L.mdrl_fit_tables.argtypes = [st, st, st, st, st, _F]
+    L.mdrl_fit_tables_bin_local.argtypes = [st, st, st, st, st, _F]
+    L.mdrl_get_table_form.argtypes = [vp, _I]
     L.mdrl_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
     L.mdrl_destroy.argtypes = [vp]
     L.mdrl_set_tables.argtypes = [vp, st, st, st, st, st, _F, st]
@@ -165,7 +169,7 @@ def lib() -> C.CDLL:
                  "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
                  "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
         getattr(L, name).restype = st
-    for name in ("mdrl_fit_tables", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
+    for name in ("mdrl_fit_tables", "mdrl_fit_tables_bin_local", "mdrl_get_table_form", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
                  "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
                  "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
                  "mdrl_get_state", "mdrl_cmodel_run", "mdrl_time_force", "mdrl_force_eval_static"):
@@ -227,10 +231,13 @@ def halfshell_offsets() -> np.ndarray:
     return out
 
 
-def fit_tables(order: int, nseg: int, bins: int, min_log2: int, samples: int = 8) -> np.ndarray:
-    """FP64-fitted unit tables, shape (6, order+1, nseg*bins) (host only, no GPU)."""
+def fit_tables(order: int, nseg: int, bins: int, min_log2: int, samples: int = 8,
+               local: bool = False) -> np.ndarray:
+    """FP64-fitted unit tables, shape (6, order+1, nseg*bins) (host only, no GPU): monomial in r2,
+    or with local=True coefficients of u = r2 - bin start (orders 2-3)."""
     out = np.zeros((6, order + 1, nseg * bins), dtype=np.float32)
-    _check(lib().mdrl_fit_tables(order, nseg, bins, min_log2, samples, _fp(out)))
+    fn = lib().mdrl_fit_tables_bin_local if local else lib().mdrl_fit_tables
+    _check(fn(order, nseg, bins, min_log2, samples, _fp(out)))
     return out
 
 
@@ -265,13 +272,17 @@ class Context:
         _check(lib().mdrl_get_tables(self._h, C.byref(o), C.byref(s), C.byref(b), C.byref(m), None))
         out = np.zeros((6, o.value + 1, s.value * b.value), dtype=np.float32)
         _check(lib().mdrl_get_tables(self._h, None, None, None, None, _fp(out)))
-        return out, {"order": o.value, "nseg": s.value, "bins": b.value, "min_log2": m.value}
+        form = C.c_int()
+        _check(lib().mdrl_get_table_form(self._h, C.byref(form)))
+        return out, {"order": o.value, "nseg": s.value, "bins": b.value, "min_log2": m.value,
+                     "raw": bool(form.value & TABLE_RAW), "local": bool(form.value & TABLE_BIN_LOCAL)}
 
     def set_tables(self, coef: np.ndarray, order: int, nseg: int, bins: int, min_log2: int,
-                   raw: bool = False) -> None:
+                   raw: bool = False, local: bool = False) -> None:
         coef = np.ascontiguousarray(coef, dtype=np.float32)
         nfunc = coef.shape[0]
-        _check(lib().mdrl_set_tables(self._h, order, nseg, bins, min_log2, nfunc, _fp(coef), int(raw)))
+        flags = (TABLE_RAW if raw else 0) | (TABLE_BIN_LOCAL if local else 0)
+        _check(lib().mdrl_set_tables(self._h, order, nseg, bins, min_log2, nfunc, _fp(coef), flags))
 
     def set_pme(self, enable: bool = True, **kw) -> dict:
         """Switch smooth-PME long-range electrostatics on (keywords: beta, tolerance, spacing,

@@ -25,6 +25,39 @@ using namespace mdrl;
 namespace mdrl {
 static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
+
+/* The armed fault: calls whose text starts with g_fault_call count down g_fault_left; the one that
+ * takes it to zero fails. */
+static std::mutex g_fault_mu;
+static std::string g_fault_call;
+static int g_fault_left = 0;
+
+void fault_arm_from_env(bool at_create) {
+    std::lock_guard<std::mutex> lock(g_fault_mu);
+    g_fault_call.clear();
+    g_fault_left = 0;
+    const char *v = getenv("MDRL_FAULT");
+    if (!v || !*v) return;
+    std::string spec(v);
+    const bool create = spec.compare(0, 7, "create:") == 0;
+    if (create) spec = spec.substr(7);
+    if (create != at_create) return;
+    int k = 1;
+    const size_t at = spec.find('@');
+    if (at != std::string::npos) {
+        k = atoi(spec.c_str() + at + 1);
+        spec = spec.substr(0, at);
+    }
+    if (spec.empty() || k < 1) return;
+    g_fault_call = spec;
+    g_fault_left = k;
+}
+
+bool fault_hit(const char *call_text) {
+    std::lock_guard<std::mutex> lock(g_fault_mu);
+    if (g_fault_left <= 0 || strncmp(call_text, g_fault_call.c_str(), g_fault_call.size()) != 0) return false;
+    return --g_fault_left == 0;
+}
 }  // namespace mdrl
 
 extern "C" const char *mdrl_version(void) { return "mdrl 0.1 (sm_103a)"; }
@@ -60,7 +93,7 @@ extern "C" void mdrl_default_params(mdrl_params *p) {
 
 static int ilog2i(int v) { int l = 0; while ((1 << l) < v) ++l; return l; }
 
-static mdrl_status validate(const mdrl_params *p) {
+mdrl_status mdrl::validate_params(const mdrl_params *p) {
     char buf[256];
     for (int d = 0; d < 3; ++d)
         if (!(p->box[d] > 0.0) || !std::isfinite(p->box[d])) {
@@ -81,6 +114,10 @@ static mdrl_status validate(const mdrl_params *p) {
             set_error(buf);
             return MDRL_ERR_INVALID_ARG;
         }
+    if (!std::isfinite(p->coulomb_k) || std::fabs(p->coulomb_k) > 1.0e30) {
+        set_error("coulomb_k must be finite");
+        return MDRL_ERR_INVALID_ARG;
+    }
     if (p->table_order < 1 || p->table_order > 3) {
         set_error("table_order must be 1, 2 or 3");
         return MDRL_ERR_INVALID_ARG;
@@ -111,6 +148,10 @@ static mdrl_status validate(const mdrl_params *p) {
     }
     if (!(p->dt_fs > 0.0) || !std::isfinite(p->dt_fs)) {
         set_error("dt_fs must be positive");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if ((p->flags & MDRL_FLAG_EXACT_DIFF) && p->arith != MDRL_ARITH_FMA) {
+        set_error("MDRL_FLAG_EXACT_DIFF needs MDRL_ARITH_FMA");
         return MDRL_ERR_INVALID_ARG;
     }
     return MDRL_OK;
@@ -213,6 +254,7 @@ TableDev mdrl::table_dev(const mdrl_ctx *c) {
     t.order = c->order; t.nseg = c->nseg; t.bins = c->bins; t.lb = ilog2i(c->bins);
     t.min_log2 = c->min_log2;
     t.r2min = std::ldexp(1.0f, c->min_log2);
+    t.local = c->local ? 1 : 0;
     return t;
 }
 
@@ -225,7 +267,8 @@ static int segments_for(float rc2, int min_log2) {
 extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
     if (!p || !out) { set_error("null argument"); return MDRL_ERR_INVALID_ARG; }
     *out = nullptr;
-    MDRL_TRY(validate(p));
+    fault_arm_from_env(true);
+    MDRL_TRY(validate_params(p));
     int ndev = 0;
     MDRL_CUDA(cudaGetDeviceCount(&ndev));
     if (p->device < 0 || p->device >= ndev) { set_error("device ordinal out of range"); return MDRL_ERR_INVALID_ARG; }
@@ -243,7 +286,8 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
         return MDRL_ERR_RANGE;
     }
     c->ke = (float)p->coulomb_k;
-    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab);
+    c->local = c->order >= 2;    /* the library's own order-2/3 tables are bin-local */
+    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab, 0.0, c->local);
     mix_pair_coefficients(*p, &c->pcoef, nullptr);
     const double conv = 4.184e-4; /* (kcal/mol/A)/amu -> A/fs^2 */
     for (int t = 0; t < MDRL_MAX_TYPES; ++t) {
@@ -276,6 +320,7 @@ extern "C" mdrl_status mdrl_create(const mdrl_params *p, mdrl_ctx **out) {
         return MDRL_ERR_CUDA;
     }
     *out = c;
+    fault_arm_from_env(false);
     return MDRL_OK;
 }
 
@@ -285,6 +330,7 @@ static void free_particles(mdrl_ctx *c) {
     dfree(&c->d_ovx); dfree(&c->d_ovy); dfree(&c->d_ovz); dfree(&c->d_ocnt);
     for (int b = 0; b < 2; ++b) { dfree(&c->d_pos[b]); dfree(&c->d_vel[b]); dfree(&c->d_type[b]); dfree(&c->d_id[b]); }
     dfree(&c->d_cell_of); dfree(&c->d_slot); dfree(&c->d_tmp); dfree(&c->d_sorted); dfree(&c->d_key);
+    dfree(&c->d_sortkey);
     dfree(&c->d_F64); dfree(&c->d_F32); dfree(&c->d_cnt);
     dfree(&c->d_Fscr64); dfree(&c->d_Fscr32);
     c->cap = 0;
@@ -342,6 +388,7 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
     }
     MDRL_TRY(dalloc(&c->d_cell_of, m)); MDRL_TRY(dalloc(&c->d_slot, m));
     MDRL_TRY(dalloc(&c->d_tmp, m)); MDRL_TRY(dalloc(&c->d_sorted, m)); MDRL_TRY(dalloc(&c->d_key, m));
+    MDRL_TRY(dalloc(&c->d_sortkey, m));
     if (c->p.accum == MDRL_ACC_FIXED64) { MDRL_TRY(dalloc(&c->d_F64, 3 * m)); }
     else { MDRL_TRY(dalloc(&c->d_F32, 6 * m)); }   /* high and low planes */
     MDRL_TRY(dalloc(&c->d_cnt, m));
@@ -357,13 +404,21 @@ mdrl_status mdrl::ensure_capacity(mdrl_ctx *c, int n) {
 /* ---- kernel dispatch ---------------------------------------------------------------------- */
 
 namespace mdrl {
-force_fn pick_force(int order, bool sep, bool extra, int acc, int fw, bool prune) {
-    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false>(order, sep, extra);
-    if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false>(order, sep, extra);
-    if (fw == 8) return prune ? pick_force_set<0, 8, true>(order, sep, extra)
-                              : pick_force_set<0, 8, false>(order, sep, extra);
-    return prune ? pick_force_set<0, 4, true>(order, sep, extra)
-                 : pick_force_set<0, 4, false>(order, sep, extra);
+force_fn pick_force(int order, bool sep, bool extra, int acc, int fw, bool prune, bool exact) {
+    if (exact) {
+        if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false, kDiffExact>(order, false, extra);
+        if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false, kDiffExact>(order, false, extra);
+        if (fw == 8) return prune ? pick_force_set<0, 8, true, kDiffExact>(order, false, extra)
+                                  : pick_force_set<0, 8, false, kDiffExact>(order, false, extra);
+        return prune ? pick_force_set<0, 4, true, kDiffExact>(order, false, extra)
+                     : pick_force_set<0, 4, false, kDiffExact>(order, false, extra);
+    }
+    if (acc == MDRL_ACC_FP32_ATOMIC) return pick_force_set<1, 4, false, kDiffShift>(order, sep, extra);
+    if (acc == MDRL_ACC_KAHAN) return pick_force_set<2, 4, false, kDiffShift>(order, sep, extra);
+    if (fw == 8) return prune ? pick_force_set<0, 8, true, kDiffShift>(order, sep, extra)
+                              : pick_force_set<0, 8, false, kDiffShift>(order, sep, extra);
+    return prune ? pick_force_set<0, 4, true, kDiffShift>(order, sep, extra)
+                 : pick_force_set<0, 4, false, kDiffShift>(order, sep, extra);
 }
 
 force_fn pick_force_batch(int order, bool sep, bool extra, bool prune) {
@@ -391,14 +446,15 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
                                      unsigned long long *F64, float *F32) {
     const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
     const bool prune = c->p.accum == MDRL_ACC_FIXED64 && c->tile.prune_steps;
-    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, fw, prune);
+    force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, fw, prune,
+                             (c->p.flags & MDRL_FLAG_EXACT_DIFF) != 0);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const int units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
                                              c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr,
-                                             tile_word(c->tile.steps_per_piece, c->tile.prune_steps));
+                                             tile_word(c->tile.steps_per_piece, c->tile.prune_steps), c->d_err);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -437,7 +493,7 @@ static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, 
     if (n > 0) {
         k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
         k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted,
-                                                       spatial ? c->d_key : nullptr);
+                                                       spatial ? c->d_key : nullptr, c->d_sortkey, c->d_err);
         k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, x, y, z, q, type, c->d_pos[buf],
                                                            c->d_type[buf], c->d_id[buf], c->d_F64,
                                                            c->d_F32, c->d_cnt, c->p.ntypes, c->d_err,
@@ -447,9 +503,7 @@ static mdrl_status bin_user(mdrl_ctx *c, int n, const float *x, const float *y, 
     return MDRL_OK;
 }
 
-mdrl_status mdrl::check_device_errors(mdrl_ctx *c) {
-    unsigned err = 0;
-    MDRL_CUDA(cudaMemcpy(&err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+mdrl_status mdrl::device_error_status(unsigned err) {
     if (err & kErrPosition) {
         set_error("positions must be finite and lie in [0, box) on every axis");
         return MDRL_ERR_INVALID_ARG;
@@ -458,7 +512,23 @@ mdrl_status mdrl::check_device_errors(mdrl_ctx *c) {
         set_error("particle types must lie in [0, ntypes)");
         return MDRL_ERR_INVALID_ARG;
     }
+    if (err & kErrCellOverflow) {
+        set_error("a cell holds more than 65536 particles (the largest occupancy the in-cell sort and "
+                  "the force kernel accept); the units that touch it were skipped");
+        return MDRL_ERR_CELL_OVERFLOW;
+    }
+    if (err & kErrForce) {
+        set_error("a force component was NaN or infinite, or (int64 fixed point) reached 5.4e11 "
+                  "kcal/mol/A, beyond what the accumulators hold");
+        return MDRL_ERR_RANGE;
+    }
     return MDRL_OK;
+}
+
+mdrl_status mdrl::check_device_errors(mdrl_ctx *c) {
+    unsigned err = 0;
+    MDRL_CUDA(cudaMemcpy(&err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return device_error_status(err);
 }
 
 static mdrl_status read_stats(mdrl_ctx *c, mdrl_stats *st, float ms) {
@@ -533,15 +603,7 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
 }
 
 static mdrl_status force_eval_finish(mdrl_ctx *c, mdrl_stats *st) {
-    const unsigned err = *c->h_err;
-    if (err & kErrPosition) {
-        set_error("positions must be finite and lie in [0, box) on every axis");
-        return MDRL_ERR_INVALID_ARG;
-    }
-    if (err & kErrType) {
-        set_error("particle types must lie in [0, ntypes)");
-        return MDRL_ERR_INVALID_ARG;
-    }
+    MDRL_TRY(device_error_status(*c->h_err));
     if (!st) return MDRL_OK;
     const DevTotals &t = *c->h_tot;
     memset(st, 0, sizeof(*st));
@@ -658,10 +720,19 @@ extern "C" mdrl_status mdrl_bin(mdrl_ctx *c, int n, const float *x, const float 
 /* ---- tables ------------------------------------------------------------------------------- */
 
 extern "C" mdrl_status mdrl_set_tables(mdrl_ctx *c, int order, int nseg, int bins, int min_log2,
-                                       int nfunc, const float *coef, int raw) {
+                                       int nfunc, const float *coef, int flags) {
     if (!c || !coef || order < 1 || order > 3 || nseg < 1 || bins < 16 || bins > 4096 ||
-        (bins & (bins - 1)) || (nfunc != 2 && nfunc != 3 && nfunc != 6)) {
+        (bins & (bins - 1)) || (nfunc != 2 && nfunc != 3 && nfunc != 6) ||
+        (flags & ~(MDRL_TABLE_RAW | MDRL_TABLE_BIN_LOCAL))) {
         set_error("mdrl_set_tables: invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if ((flags & MDRL_TABLE_BIN_LOCAL) && order < 2) {
+        set_error("mdrl_set_tables: the bin-local form is for orders 2 and 3");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (min_log2 < -30 || min_log2 > 20 || nseg > 64) {
+        set_error("mdrl_set_tables: min_log2 must be in -30..20 and nseg at most 64");
         return MDRL_ERR_INVALID_ARG;
     }
     const double top = std::ldexp(1.0, min_log2 + nseg);
@@ -672,7 +743,8 @@ extern "C" mdrl_status mdrl_set_tables(mdrl_ctx *c, int order, int nseg, int bin
     MDRL_CUDA(cudaSetDevice(c->p.device));
     const int nidx = nseg * bins, nc = order + 1;
     c->order = order; c->nseg = nseg; c->bins = bins; c->min_log2 = min_log2;
-    c->raw = raw != 0;
+    c->raw = (flags & MDRL_TABLE_RAW) != 0;
+    c->local = (flags & MDRL_TABLE_BIN_LOCAL) != 0;
     c->tab.assign((size_t)kNumFunc * nc * nidx, 0.0f);
     memcpy(c->tab.data(), coef, sizeof(float) * (size_t)nfunc * nc * nidx);
     for (int k = 0; k < 2; ++k) {
@@ -691,6 +763,12 @@ extern "C" mdrl_status mdrl_get_tables(mdrl_ctx *c, int *order, int *nseg, int *
     if (bins) *bins = c->bins;
     if (min_log2) *min_log2 = c->min_log2;
     if (coef) memcpy(coef, c->tab.data(), sizeof(float) * c->tab.size());
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_get_table_form(mdrl_ctx *c, int *flags) {
+    if (!c || !flags) { set_error("mdrl_get_table_form: null argument"); return MDRL_ERR_INVALID_ARG; }
+    *flags = (c->raw ? MDRL_TABLE_RAW : 0) | (c->local ? MDRL_TABLE_BIN_LOCAL : 0);
     return MDRL_OK;
 }
 
@@ -724,22 +802,34 @@ extern "C" mdrl_status mdrl_set_pair_coefficients(mdrl_ctx *c, const double *coe
     return MDRL_OK;
 }
 
-extern "C" mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples,
-                                       float *coef) {
-    if (!coef || order < 1 || order > 3 || nseg < 1 || bins < 1 || samples < order + 1 || samples > 1024) {
-        set_error("mdrl_fit_tables: invalid argument");
+static mdrl_status fit_tables_checked(int order, int nseg, int bins, int min_log2, int samples, float *coef,
+                                      bool local, const char *who) {
+    if (!coef || order < 1 || order > 3 || nseg < 1 || nseg > 64 || bins < 1 || bins > 4096 ||
+        (bins & (bins - 1)) || samples < order + 1 || samples > 1024 || min_log2 < -30 || min_log2 > 20 ||
+        (local && order < 2)) {
+        set_error(std::string(who) + ": invalid argument");
         return MDRL_ERR_INVALID_ARG;
     }
     std::vector<float> t;
-    fit_tables(order, nseg, bins, min_log2, samples, &t);
+    fit_tables(order, nseg, bins, min_log2, samples, &t, 0.0, local);
     memcpy(coef, t.data(), sizeof(float) * t.size());
     return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_fit_tables(int order, int nseg, int bins, int min_log2, int samples,
+                                       float *coef) {
+    return fit_tables_checked(order, nseg, bins, min_log2, samples, coef, false, "mdrl_fit_tables");
+}
+
+extern "C" mdrl_status mdrl_fit_tables_bin_local(int order, int nseg, int bins, int min_log2, int samples,
+                                                 float *coef) {
+    return fit_tables_checked(order, nseg, bins, min_log2, samples, coef, true, "mdrl_fit_tables_bin_local");
 }
 
 /* ---- per-pair plugin ---------------------------------------------------------------------- */
 
 typedef void (*pair_fn)(int, const float4 *, const float4 *, const int *, const int *, Geom, TableDev,
-                        const float4 *, int, float, float4 *, float2 *);
+                        const float4 *, int, float, float4 *, float2 *, int);
 
 static pair_fn pick_pair(int order, bool sep) {
     switch (order) {
@@ -773,7 +863,8 @@ extern "C" mdrl_status mdrl_pair_eval(mdrl_ctx *c, int n, const float *ref, cons
     pair_fn fn = pick_pair(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE);
     fn<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_pr, c->d_pn, tref ? c->d_ptr : nullptr,
                                             tnbr ? c->d_ptn : nullptr, g, table_dev(c), c->d_pcoef,
-                                            c->p.ntypes, c->ke, c->d_pout, aux ? c->d_paux : nullptr);
+                                            c->p.ntypes, c->ke, c->d_pout, aux ? c->d_paux : nullptr,
+                                            (c->p.flags & MDRL_FLAG_EXACT_DIFF) ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaMemcpyAsync(out, c->d_pout, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream));
     if (aux) MDRL_CUDA(cudaMemcpyAsync(aux, c->d_paux, sizeof(float2) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -840,7 +931,8 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
                                                           c->d_count, c->d_key);
     k_scan<<<1, 1024, 0, c->stream>>>(c->ncells, c->d_count, c->d_start, c->d_tot);
     k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
-    k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key);
+    k_cell_sort<<<c->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key, c->d_sortkey,
+                                                   c->d_err);
     k_gather_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, c->d_pos[a], c->d_vel[a], c->d_type[a],
                                                         c->d_id[a], c->d_pos[b], c->d_vel[b], c->d_type[b],
                                                         c->d_id[b], c->d_F64, c->d_F32);
@@ -867,6 +959,7 @@ extern "C" mdrl_status mdrl_step(mdrl_ctx *c, int nsteps, mdrl_stats *st) {
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, offsetof(DevTotals, pairs_total), c->stream));
     MDRL_CUDA(cudaMemsetAsync(&c->d_tot->pairs_total, 0, sizeof(unsigned long long), c->stream));
+    MDRL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
     if (c->graph_n != c->n || c->graph_extra != extra) {
         /* Capture one step per buffer parity (slot 0 -> 1 and slot 1 -> 0). */
         const int saved = c->cur;
@@ -896,7 +989,8 @@ extern "C" mdrl_status mdrl_step(mdrl_ctx *c, int nsteps, mdrl_stats *st) {
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     float ms = 0.0f;
     MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    return read_stats(c, st, ms);
+    MDRL_TRY(read_stats(c, st, ms));
+    return check_device_errors(c);
 }
 
 extern "C" mdrl_status mdrl_time_force(mdrl_ctx *c, float *ms) {
@@ -1101,6 +1195,7 @@ extern "C" mdrl_status mdrl_set_pme(mdrl_ctx *c, const mdrl_pme_params *p) {
     }
     /* the Coulomb slots: Ewald real-space pair with PME, plain r^-3 / r^-1 without */
     c->raw = false;
-    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab, beta);
+    c->local = c->order >= 2;
+    fit_tables(c->order, c->nseg, c->bins, c->min_log2, 8, &c->tab, beta, c->local);
     return upload_tables(c);
 }

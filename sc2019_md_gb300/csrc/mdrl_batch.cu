@@ -215,6 +215,11 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
         set_error("mdrl_batch_create: replicas are periodic (MDRL_FLAG_NO_PBC is not supported)");
         return MDRL_ERR_INVALID_ARG;
     }
+    if (p->flags & MDRL_FLAG_EXACT_DIFF) {
+        set_error("mdrl_batch_create: MDRL_FLAG_EXACT_DIFF is for single systems (the small-box replica "
+                  "paths use the reference's difference rule)");
+        return MDRL_ERR_INVALID_ARG;
+    }
     std::vector<BatchRep> hrep(nrep);
     long long ntot = 0, ncells = 0;
     for (int r = 0; r < nrep; ++r) {
@@ -329,7 +334,7 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<b->nitems, kBatchFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
                                                   c->p.ntypes, c->ke, b->ntot, F64, nullptr, c->d_cnt, c->d_unit,
-                                                  b->d_items, b->d_reps, tile_word(c->tile.steps_per_piece, c->tile.prune_steps));
+                                                  b->d_items, b->d_reps, tile_word(c->tile.steps_per_piece, c->tile.prune_steps), c->d_err);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -345,7 +350,8 @@ static mdrl_status batch_bin_user(mdrl_batch *b, const float *q, const int *type
                                                      c->d_cell_of, c->d_slot, c->d_count, c->d_err, c->d_key);
     k_scan<<<1, 1024, 0, c->stream>>>(b->ncells, c->d_count, c->d_start, c->d_tot);
     k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
-    k_cell_sort<<<b->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key);
+    k_cell_sort<<<b->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key, c->d_sortkey,
+                                                   c->d_err);
     k_gather_user<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, c->d_ux, c->d_uy, c->d_uz, q, type,
                                                        c->d_pos[buf], c->d_type[buf], c->d_id[buf], c->d_F64,
                                                        nullptr, c->d_cnt, c->p.ntypes, c->d_err);
@@ -472,7 +478,8 @@ static mdrl_status batch_enqueue_step(mdrl_batch *b, bool extra) {
                                                            c->d_count, c->d_key);
     k_scan<<<1, 1024, 0, c->stream>>>(b->ncells, c->d_count, c->d_start, c->d_tot);
     k_scatter<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_cell_of, c->d_slot, c->d_start, c->d_tmp);
-    k_cell_sort<<<b->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key);
+    k_cell_sort<<<b->ncells, 128, 0, c->stream>>>(c->d_start, c->d_tmp, c->d_sorted, c->d_key, c->d_sortkey,
+                                                   c->d_err);
     k_gather_state<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_sorted, c->d_pos[a], c->d_vel[a], c->d_type[a],
                                                         c->d_id[a], c->d_pos[d], c->d_vel[d], c->d_type[d],
                                                         c->d_id[d], c->d_F64, nullptr);
@@ -495,6 +502,7 @@ extern "C" mdrl_status mdrl_batch_step(mdrl_batch *b, int nsteps, mdrl_stats *st
     const bool extra = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, offsetof(DevTotals, pairs_total), c->stream));
     MDRL_CUDA(cudaMemsetAsync(&c->d_tot->pairs_total, 0, sizeof(unsigned long long), c->stream));
+    MDRL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
     if (c->graph_n != b->ntot || c->graph_extra != extra) {
         const int saved = c->cur;
         for (int k = 0; k < 2; ++k) {
@@ -523,7 +531,8 @@ extern "C" mdrl_status mdrl_batch_step(mdrl_batch *b, int nsteps, mdrl_stats *st
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     float ms = 0.0f;
     MDRL_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    return batch_read_totals(b, st, ms);
+    MDRL_TRY(batch_read_totals(b, st, ms));
+    return check_device_errors(c);
 }
 
 extern "C" mdrl_status mdrl_batch_get_state(mdrl_batch *b, float *x, float *y, float *z, float *vx, float *vy,

@@ -105,14 +105,16 @@ __device__ __forceinline__ float3 bscale(float s, float3 a) { return make_float3
 __device__ __forceinline__ float3 badd(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
 
 template <int ACC>
-__device__ __forceinline__ void badd_force(unsigned long long *F64, float *F32, int n, int k, float3 f) {
-    flush_force<ACC>(F64, F32, n, k, f.x, f.y, f.z);
+__device__ __forceinline__ void badd_force(unsigned long long *F64, float *F32, int n, int k, float3 f,
+                                           unsigned *err) {
+    flush_force<ACC>(F64, F32, n, k, f.x, f.y, f.z, err);
 }
 
 template <int ACC>
 static __global__ void __launch_bounds__(kBondedThreads)
 k_bonded(BondedDev b, int n, const int *__restrict__ inv, const float4 *__restrict__ pos, Geom g,
-         unsigned long long *__restrict__ F64, float *__restrict__ F32, double *__restrict__ epart) {
+         unsigned long long *__restrict__ F64, float *__restrict__ F32, double *__restrict__ epart,
+         unsigned *__restrict__ err) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     float eb = 0.0f, ea = 0.0f, ed = 0.0f;
     if (t < b.nb) {
@@ -131,8 +133,8 @@ k_bonded(BondedDev b, int n, const int *__restrict__ inv, const float4 *__restri
         eb = p.x * dd * dd;
         if (d > 0.0f) {
             const float3 fi = bscale(-2.0f * p.x * dd / d, r);
-            badd_force<ACC>(F64, F32, n, i, fi);
-            badd_force<ACC>(F64, F32, n, j, bscale(-1.0f, fi));
+            badd_force<ACC>(F64, F32, n, i, fi, err);
+            badd_force<ACC>(F64, F32, n, j, bscale(-1.0f, fi), err);
         }
     } else if (t < b.nb + b.na) {
         const int4 at = b.ai[t - b.nb];
@@ -162,9 +164,9 @@ k_bonded(BondedDev b, int n, const int *__restrict__ inv, const float4 *__restri
             f1 = make_float3(f1.x - ub.x, f1.y - ub.y, f1.z - ub.z);
             f3 = badd(f3, ub);
         }
-        badd_force<ACC>(F64, F32, n, i, f1);
-        badd_force<ACC>(F64, F32, n, l, f3);
-        badd_force<ACC>(F64, F32, n, j, bscale(-1.0f, badd(f1, f3)));
+        badd_force<ACC>(F64, F32, n, i, f1, err);
+        badd_force<ACC>(F64, F32, n, l, f3, err);
+        badd_force<ACC>(F64, F32, n, j, bscale(-1.0f, badd(f1, f3)), err);
     } else if (t < b.nb + b.na + b.nd) {
         const int4 at = b.di[t - b.nb - b.na];
         const float4 p = b.dp[t - b.nb - b.na];
@@ -195,10 +197,10 @@ k_bonded(BondedDev b, int n, const int *__restrict__ inv, const float4 *__restri
             const float3 d1 = bscale(-ca, A), d4 = bscale(cb, B);
             const float3 d2 = make_float3((ca + sa) * A.x - sb * B.x, (ca + sa) * A.y - sb * B.y, (ca + sa) * A.z - sb * B.z);
             const float3 d3 = make_float3((sb - cb) * B.x - sa * A.x, (sb - cb) * B.y - sa * A.y, (sb - cb) * B.z - sa * A.z);
-            badd_force<ACC>(F64, F32, n, a1, bscale(-dpot, d1));
-            badd_force<ACC>(F64, F32, n, a2, bscale(-dpot, d2));
-            badd_force<ACC>(F64, F32, n, a3, bscale(-dpot, d3));
-            badd_force<ACC>(F64, F32, n, a4, bscale(-dpot, d4));
+            badd_force<ACC>(F64, F32, n, a1, bscale(-dpot, d1), err);
+            badd_force<ACC>(F64, F32, n, a2, bscale(-dpot, d2), err);
+            badd_force<ACC>(F64, F32, n, a3, bscale(-dpot, d3), err);
+            badd_force<ACC>(F64, F32, n, a4, bscale(-dpot, d4), err);
         }
     }
     if (!epart) return;
@@ -262,13 +264,13 @@ mdrl_status bonded_enqueue(mdrl_ctx *c, int n, const float4 *pos, const int *pid
     double *ep = energy ? s->d_epart : nullptr;
     switch (c->p.accum) {
     case MDRL_ACC_FP32_ATOMIC:
-        k_bonded<1><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep);
+        k_bonded<1><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep, c->d_err);
         break;
     case MDRL_ACC_KAHAN:
-        k_bonded<2><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep);
+        k_bonded<2><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep, c->d_err);
         break;
     default:
-        k_bonded<0><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep);
+        k_bonded<0><<<blocks, kBondedThreads, 0, c->stream>>>(b, n, c->d_inv, pos, c->g, F64, F32, ep, c->d_err);
     }
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;

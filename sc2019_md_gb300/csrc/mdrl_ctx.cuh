@@ -21,6 +21,10 @@ struct BondedState;
 
 #define MDRL_CUDA(call)                                                                   \
     do {                                                                                  \
+        if (mdrl::fault_hit(#call)) {                                                     \
+            set_error(std::string(#call) + ": injected failure (MDRL_FAULT)");           \
+            return MDRL_ERR_CUDA;                                                         \
+        }                                                                                 \
         cudaError_t e_ = (call);                                                          \
         if (e_ != cudaSuccess) {                                                          \
             set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                \
@@ -62,6 +66,7 @@ struct mdrl_ctx {
     /* tables */
     int order = 1, nseg = 0, bins = 256, min_log2 = -2;
     bool raw = false;
+    bool local = false;          /* coefficients in u = r2 - bin start (MDRL_TABLE_BIN_LOCAL) */
     std::vector<float> tab;      /* canonical [6][order+1][nseg*bins] */
     std::vector<float> pcoef;    /* [T*T*4] */
     float ke = 0.0f;
@@ -86,6 +91,7 @@ struct mdrl_ctx {
     int *d_cell_of = nullptr, *d_slot = nullptr, *d_tmp = nullptr, *d_sorted = nullptr;
     int *d_count = nullptr, *d_start = nullptr;
     unsigned *d_key = nullptr;   /* in-cell sort key (Morton code inside the cell) */
+    unsigned long long *d_sortkey = nullptr;   /* sorted chunks of cells above kSortSmall */
     unsigned long long *d_F64 = nullptr;
     float *d_F32 = nullptr;
     unsigned long long *d_Fscr64 = nullptr; /* scratch accumulators for mdrl_time_force */
@@ -128,6 +134,7 @@ mdrl_status ensure_capacity(mdrl_ctx *c, int n);
 TableDev table_dev(const mdrl_ctx *c);
 int eff_order(const mdrl_ctx *c);
 mdrl_status check_device_errors(mdrl_ctx *c);
+
 /* Raise the dynamic shared-memory limit of a force kernel once per kernel and device. */
 mdrl_status prepare_force_kernel(force_fn fn, int device);
 inline int nblk(int n, int b) { return (n + b - 1) / b; }

@@ -66,13 +66,15 @@ struct BatchRep;
 struct BatchItem;
 typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
                          int, float, int, unsigned long long *, float *, int *, UnitOut *,
-                         const BatchItem *, const BatchRep *, int);
+                         const BatchItem *, const BatchRep *, int, unsigned *);
 
 /* Work items (one per unit): the result slots k_totals sums. */
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
 
-/* fw: warps per CTA (8 only with int64 fixed point); prune: survivor lists (fixed point only) */
-force_fn pick_force(int order, bool sep, bool extra, int acc, int fw = kFW, bool prune = false);
+/* fw: warps per CTA (8 only with int64 fixed point); prune: survivor lists (fixed point only);
+ * exact: the exact-difference rule (fused arithmetic only) */
+force_fn pick_force(int order, bool sep, bool extra, int acc, int fw = kFW, bool prune = false,
+                    bool exact = false);
 /* the batched-replica instantiation (int64 fixed point, difference rule per item) */
 force_fn pick_force_batch(int order, bool sep, bool extra, bool prune);
 
@@ -107,26 +109,35 @@ __device__ __forceinline__ void pair_functions_fast(const TableDev &t, float r2,
             if (coul) { const float2 gg = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(gg.y, r2e, gg.x); }
         }
     } else {
-        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), r2e);
-        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), r2e);
-        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), r2e) : 0.0f;
+        const float x = table_variable(t, r2e);
+        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), x);
+        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), x);
+        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), x) : 0.0f;
         if (ENERGY) {
-            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), r2e);
-            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), r2e);
-            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), r2e) : 0.0f;
+            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), x);
+            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), x);
+            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), x) : 0.0f;
         }
     }
 }
 
-/* Pair difference rules of a unit (both give the reference's d for every pair that can pass the
- * filter; see the header):
+/* Pair difference rules of a unit (the first two give the reference's d for every pair that can
+ * pass the filter; see the header):
  *   kDiffShift  fl(fl(xi - xj) + s)        (the unit's -L/0/+L shift: half-shell units)
- *   kDiffWrap   the one-wrap rule per pair (explicit cell pairs of small boxes in batches) */
-enum : int { kDiffShift = 1, kDiffWrap = 2 };
+ *   kDiffWrap   the one-wrap rule per pair (explicit cell pairs of small boxes in batches)
+ *   kDiffExact  fl(xi' - xj'): the exact minimum-image difference rounded once
+ *               (MDRL_FLAG_EXACT_DIFF).  The unit's shift is taken off the far (high) coordinate
+ *               when the cells are staged: across the +L face the home cell is the last one, so
+ *               xi' = xi - L (exact: xi >= 2L/3 with at least 3 cells, Sterbenz); across the -L
+ *               face the neighbour is the last cell and xj' = xj - L.  The reference's rule
+ *               rounds fl(xi - xj) of two far-apart coordinates first, an absolute error up to
+ *               ulp(L)/2 that r^-14 amplifies 14-fold in a close pair's force. */
+enum : int { kDiffShift = 1, kDiffWrap = 2, kDiffExact = 3 };
 
 template <int MODE>
 __device__ __forceinline__ float pair_diff(float a, float b, float L, float h, float s) {
     const float d = __fsub_rn(a, b);
+    if (MODE == kDiffExact) return d;
     return MODE == kDiffWrap ? wrap_d(d, L, h) : __fadd_rn(d, s);
 }
 
@@ -198,9 +209,13 @@ __device__ __forceinline__ void kahan_add(float *hi, float *lo, float v) {
     if (e != 0.0f) atomicAdd(lo, e);
 }
 
+/* Add one particle's force (fx, fy, fz) to the accumulators of mode ACC.  A sum the mode cannot
+ * hold (NaN or infinite; with fixed point also |F| >= kFixMax) raises kErrForce in *err. */
 template <int ACC>
 __device__ __forceinline__ void flush_force(unsigned long long *F64, float *F32, int n, int g, float fx,
-                                            float fy, float fz) {
+                                            float fy, float fz, unsigned *err) {
+    if (ACC == 0) check_force(err, fx, fy, fz);
+    else if (!(isfinite(fx) && isfinite(fy) && isfinite(fz)) && err) atomicOr(err, kErrForce);
     if (ACC == 1) {
         atomicAdd(F32 + g, fx);
         atomicAdd(F32 + n + g, fy);
@@ -253,7 +268,7 @@ __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, 
                                                    unsigned long long *__restrict__ F64,
                                                    int *__restrict__ counts, float4 *sJp, int *sJt,
                                                    float &acc_elj, float &acc_ec, float &acc_vir,
-                                                   unsigned &acc_pairs, unsigned &acc_below) {
+                                                   unsigned &acc_pairs, unsigned &acc_below, unsigned *err) {
     const Geom &g = rp.g;
     const int tid = threadIdx.x;
     const int i = b0 + tid;
@@ -320,6 +335,7 @@ __device__ __forceinline__ void all_images_body(const float4 *__restrict__ pos, 
     }
     if (have) {
         const size_t gi = (size_t)rp.p_off + i;
+        check_force(err, fx, fy, fz);
         F64[gi] = to_fixed(fx);
         F64[(size_t)ntot + gi] = to_fixed(fy);
         F64[2 * (size_t)ntot + gi] = to_fixed(fz);
@@ -337,7 +353,8 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                                            unsigned long long *__restrict__ F64, float *__restrict__ F32,
                                            int *__restrict__ counts, UnitOut *__restrict__ uout, float4 *sIp,
                                            float4 *sJp, float4 *sCoef, int *sIt, int *sJt, float *sF, int *sC,
-                                           double (*s_red)[3], unsigned long long (*s_cnt)[2], int tilecfg) {
+                                           double (*s_red)[3], unsigned long long (*s_cnt)[2], int tilecfg,
+                                           unsigned *err) {
     const int spp = tilecfg & 0xff;               /* j-steps per piece */
     constexpr bool prune = PRUNE;                 /* survivor lists (below) */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -391,6 +408,22 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                 for (int t = tid; t < FW * 2 * kChunk / 4; t += (FW * 32))
                     reinterpret_cast<int4 *>(sC)[t] = make_int4(0, 0, 0, 0);
             cp_async_wait_all();
+            if (MODE == kDiffExact && (sx != 0.0f || sy != 0.0f || sz != 0.0f)) {
+                /* take the box edge off the high side's coordinates (exact); each thread shifts
+                 * the elements it copied, which its own wait has completed */
+                const float ix = sx < 0.0f ? sx : 0.0f, iy = sy < 0.0f ? sy : 0.0f, iz = sz < 0.0f ? sz : 0.0f;
+                const float jx = sx > 0.0f ? sx : 0.0f, jy = sy > 0.0f ? sy : 0.0f, jz = sz > 0.0f ? sz : 0.0f;
+                for (int t = tid; t < ni; t += (FW * 32)) {
+                    float4 pp = sIp[t];
+                    pp.x = __fadd_rn(pp.x, ix); pp.y = __fadd_rn(pp.y, iy); pp.z = __fadd_rn(pp.z, iz);
+                    sIp[t] = pp;
+                }
+                for (int t = tid; t < nj; t += (FW * 32)) {
+                    float4 pp = sJp[t];
+                    pp.x = __fsub_rn(pp.x, jx); pp.y = __fsub_rn(pp.y, jy); pp.z = __fsub_rn(pp.z, jz);
+                    sJp[t] = pp;
+                }
+            }
             __syncthreads();
 
             const int nti = (ni + 31) >> 5;
@@ -597,7 +630,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                     if (diag) { v0 += a[3 * kChunk + t]; v1 += a[4 * kChunk + t]; v2 += a[5 * kChunk + t]; }
                     if (EXTRA) cc += sC[w * 2 * kChunk + t] + (diag ? sC[w * 2 * kChunk + kChunk + t] : 0);
                 }
-                flush_force<ACC>(F64, F32, n, hs + i0 + t, v0, v1, v2);
+                flush_force<ACC>(F64, F32, n, hs + i0 + t, v0, v1, v2, err);
                 if (EXTRA && cc) atomicAdd(counts + hs + i0 + t, cc);
             }
             if (!diag) {
@@ -610,7 +643,7 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
                         v0 += a[t]; v1 += a[kChunk + t]; v2 += a[2 * kChunk + t];
                         if (EXTRA) cc += sC[w * 2 * kChunk + kChunk + t];
                     }
-                    flush_force<ACC>(F64, F32, n, cs + j0 + t, v0, v1, v2);
+                    flush_force<ACC>(F64, F32, n, cs + j0 + t, v0, v1, v2, err);
                     if (EXTRA && cc) atomicAdd(counts + cs + j0 + t, cc);
                 }
             }
@@ -646,13 +679,16 @@ __device__ __forceinline__ void force_unit(const float4 *__restrict__ pos, const
     }
 }
 
-template <int ORDER, bool SEP, bool EXTRA, int ACC, bool WRAP, bool BATCH = false, int FW = kFW, bool PRUNE = false>
+/* DIFF: the difference rule of half-shell units (kDiffShift, or kDiffExact for
+ * MDRL_FLAG_EXACT_DIFF); batches pick the per-pair wrap for explicit cell pairs per item. */
+template <int ORDER, bool SEP, bool EXTRA, int ACC, int DIFF, bool BATCH = false, int FW = kFW, bool PRUNE = false>
 __global__ void __launch_bounds__(FW * 32, (FW == kFW ? kFCtas : 16 / FW))
 k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         const int *__restrict__ cstart, Geom gparam, TableDev tab, const float4 *__restrict__ pcoef,
         int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
         float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout,
-        const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int tilecfg) {
+        const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int tilecfg,
+        unsigned *__restrict__ err) {
     extern __shared__ float4 smem[];
     float4 *sIp = smem;
     float4 *sJp = sIp + kChunk;
@@ -667,7 +703,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
     int unit = blockIdx.x, coff = 0;
-    bool cell_pair = false, use_wrap = WRAP;
+    bool cell_pair = false, use_wrap = false;
     Geom gb;
     if (BATCH) {
         const BatchItem it = items[blockIdx.x];
@@ -677,7 +713,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
             float e1 = 0.f, e2 = 0.f, e3 = 0.f;
             unsigned c1 = 0, c2 = 0;
             all_images_body<ORDER, SEP, EXTRA, FW>(pos, ptype, rp, it.unit, tab, sCoef, ntypes, ke, n, F64, counts,
-                                                  sJp, sJt, e1, e2, e3, c1, c2);
+                                                  sJp, sJt, e1, e2, e3, c1, c2, err);
             double d1 = e1, d2 = e2, d3 = e3;
             unsigned long long u1 = c1, u2 = c2;
 #pragma unroll
@@ -743,31 +779,43 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     }
     const int hs = cstart[coff + h], ni_all = cstart[coff + h + 1] - hs;
     const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
+    if (ni_all > kMaxCellOcc || nj_all > kMaxCellOcc) {
+        /* an overflowing cell (reported by the in-cell sort): skip the unit, bounded time */
+        if (tid == 0) {
+            UnitOut u;
+            u.e_lj = u.e_coul = u.virial = 0.0;
+            u.pairs = u.below = 0ull;
+            uout[blockIdx.x] = u;
+        }
+        return;
+    }
 #define MDRL_UNIT_ARGS pos, ptype, hs, ni_all, cs, nj_all, self, g, sx, sy, sz, tab, pcoef, ntypes, ke, n, F64, F32, \
-                       counts, uout, sIp, sJp, sCoef, sIt, sJt, sF, sC, s_red, s_cnt, tilecfg
+                       counts, uout, sIp, sJp, sCoef, sIt, sJt, sF, sC, s_red, s_cnt, tilecfg, err
     /* one unit body per kernel where the rule is fixed (a second body cost more in instruction
      * fetch than a skipped add saves); the batch picks per item */
-    if (use_wrap)
+    if (BATCH && use_wrap)
         force_unit<ORDER, SEP, EXTRA, ACC, kDiffWrap, FW, PRUNE>(MDRL_UNIT_ARGS);
     else
-        force_unit<ORDER, SEP, EXTRA, ACC, kDiffShift, FW, PRUNE>(MDRL_UNIT_ARGS);
+        force_unit<ORDER, SEP, EXTRA, ACC, DIFF, FW, PRUNE>(MDRL_UNIT_ARGS);
 #undef MDRL_UNIT_ARGS
 }
 
 /* ---- instantiation sets ----------------------------------------------------------------------
  * Each set is instantiated explicitly in one translation unit (mdrl_force_*.cu), so the sets
  * compile in parallel; everywhere else the declarations below keep them from being instantiated. */
-template <int ACC, int FW, bool PRUNE>
+/* One set: every order x extra (x arithmetic mode for the reference's difference rule; the exact
+ * rule is instantiated with fused arithmetic only). */
+template <int ACC, int FW, bool PRUNE, int DIFF>
 force_fn pick_force_set(int order, bool sep, bool extra) {
     auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return (force_fn)k_force<O, S, E, ACC, false, false, FW, PRUNE>;
+        return (force_fn)k_force<O, S, E, ACC, DIFF, false, FW, PRUNE>;
     };
     auto se = [&](auto ord) -> force_fn {
         using T = std::true_type;
         using F = std::false_type;
-        if (sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});
+        if (DIFF == kDiffShift && sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});
         return extra ? w(ord, F{}, T{}) : w(ord, F{}, F{});
     };
     switch (order) {
@@ -783,7 +831,7 @@ force_fn pick_batch_set(int order, bool sep, bool extra) {
     auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return (force_fn)k_force<O, S, E, 0, true, true, kBatchFT / 32, PRUNE>;
+        return (force_fn)k_force<O, S, E, 0, kDiffShift, true, kBatchFT / 32, PRUNE>;
     };
     auto se = [&](auto ord) -> force_fn {
         using T = std::true_type;
@@ -799,12 +847,18 @@ force_fn pick_batch_set(int order, bool sep, bool extra) {
     }
 }
 
-extern template force_fn pick_force_set<0, 4, false>(int, bool, bool);
-extern template force_fn pick_force_set<0, 4, true>(int, bool, bool);
-extern template force_fn pick_force_set<0, 8, false>(int, bool, bool);
-extern template force_fn pick_force_set<0, 8, true>(int, bool, bool);
-extern template force_fn pick_force_set<1, 4, false>(int, bool, bool);
-extern template force_fn pick_force_set<2, 4, false>(int, bool, bool);
+extern template force_fn pick_force_set<0, 4, false, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<0, 4, true, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, false, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, true, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<1, 4, false, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<2, 4, false, kDiffShift>(int, bool, bool);
+extern template force_fn pick_force_set<0, 4, false, kDiffExact>(int, bool, bool);
+extern template force_fn pick_force_set<0, 4, true, kDiffExact>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, false, kDiffExact>(int, bool, bool);
+extern template force_fn pick_force_set<0, 8, true, kDiffExact>(int, bool, bool);
+extern template force_fn pick_force_set<1, 4, false, kDiffExact>(int, bool, bool);
+extern template force_fn pick_force_set<2, 4, false, kDiffExact>(int, bool, bool);
 extern template force_fn pick_batch_set<false>(int, bool, bool);
 extern template force_fn pick_batch_set<true>(int, bool, bool);
 

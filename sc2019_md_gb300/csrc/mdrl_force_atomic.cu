@@ -6,6 +6,6 @@
 
 namespace mdrl {
 
-template force_fn pick_force_set<1, 4, false>(int, bool, bool);
+template force_fn pick_force_set<1, 4, false, kDiffShift>(int, bool, bool);
 
 }  // namespace mdrl

@@ -1,0 +1,12 @@
+/*
+ * mdrl_force_atomic_exact.cu — the force-kernel instantiations for FP32-atomic accumulation, 4 warps per CTA, with the exact-difference
+ * rule (MDRL_FLAG_EXACT_DIFF): one instantiation set per translation unit so that the sets compile
+ * in parallel.
+ */
+#include "mdrl_force.cuh"
+
+namespace mdrl {
+
+template force_fn pick_force_set<1, 4, false, kDiffExact>(int, bool, bool);
+
+}  // namespace mdrl

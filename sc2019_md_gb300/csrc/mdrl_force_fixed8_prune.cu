@@ -6,6 +6,6 @@
 
 namespace mdrl {
 
-template force_fn pick_force_set<0, 8, true>(int, bool, bool);
+template force_fn pick_force_set<0, 8, true, kDiffShift>(int, bool, bool);
 
 }  // namespace mdrl

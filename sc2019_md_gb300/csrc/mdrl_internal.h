@@ -60,12 +60,30 @@ struct DevTotals {
     double e_bond, e_angle, e_dihedral;   /* bonded terms (zero without them) */
 };
 
-/* beta > 0: the Coulomb slots hold the Ewald real-space pair (erfc-screened) instead of r^-3, r^-1 */
+/* beta > 0: the Coulomb slots hold the Ewald real-space pair (erfc-screened) instead of r^-3, r^-1;
+ * local: coefficients of u = r2 - bin start (MDRL_TABLE_BIN_LOCAL) instead of powers of r2 */
 void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out,
-                double beta = 0.0);
+                double beta = 0.0, bool local = false);
 void mix_pair_coefficients(const mdrl_params &p, std::vector<float> *pc, std::vector<double> *pc64);
 
 void set_error(const std::string &msg);
+
+/* Host validation of a parameter block (box, cutoff, types, tables, modes, time step); sets the
+ * error text and returns INVALID_ARG on the first failure. */
+mdrl_status validate_params(const mdrl_params *p);
+
+/* Host-side fault injection for tests of the error paths (no GPU fault is involved).  The
+ * environment variable MDRL_FAULT = "[create:]<call>[@k]" is read by mdrl_create (and by
+ * mdrl_force_eval_static): the k-th (default first) CUDA runtime call whose source text starts
+ * with <call> (e.g. "cudaMemcpyAsync", "cudaGraphLaunch") is not made, and the library reports it
+ * as failed with an error text that says "injected".  Without "create:" the count starts when
+ * mdrl_create returns, so the fault lands in a later entry point; with it, inside mdrl_create.
+ * One fault per arming; an empty or absent variable disarms. */
+void fault_arm_from_env(bool at_create);
+bool fault_hit(const char *call_text);
+
+/* The status (and error text) for the kernels' error word; MDRL_OK when it is zero. */
+mdrl_status device_error_status(unsigned err);
 
 }  // namespace mdrl
 

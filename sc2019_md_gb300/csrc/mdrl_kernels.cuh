@@ -28,7 +28,11 @@
 namespace mdrl {
 
 /* Tables packed for the kernels: for order 1, per table index three float2 {c0, c1} (force:
- * r^-14, r^-8, r^-3; energy: r^-12, r^-6, r^-1); for orders 2-3, three float4 {c0..c3}. */
+ * r^-14, r^-8, r^-3; energy: r^-12, r^-6, r^-1); for orders 2-3, three float4 {c0..c3}.
+ * Polynomial form: monomial in r2 (the reference's form: c0 + c1 r2 + ...), or, when `local`
+ * is set (orders 2-3), in the bin-local variable u = r2 - b0, b0 the start of r2's bin.  u is
+ * exact in FP32 (r2 and b0 share a binade and b0 <= r2 < 2 b0), so the local form carries no
+ * cancellation between large monomial terms. */
 struct TableDev {
     const float2 *f2, *e2;
     const float4 *f4, *e4;
@@ -36,13 +40,35 @@ struct TableDev {
                            {c0_14, c1_14, c0_8, c1_8}, {c0_3, c1_3, 0, 0} */
     int order, nseg, bins, lb, min_log2;
     float r2min;
+    int local;          /* orders 2-3: coefficients in u = r2 - bin start */
 };
+
+/* The polynomial variable of an in-table r2e: r2e itself, or r2e minus its bin's start (the r2
+ * bit pattern with the mantissa bits below the bin index cleared). */
+__device__ __forceinline__ float table_variable(const TableDev &t, float r2e) {
+    if (!t.local) return r2e;
+    const float b0 = __uint_as_float(__float_as_uint(r2e) & ~((1u << (23 - t.lb)) - 1u));
+    return __fsub_rn(r2e, b0);
+}
 
 /* The 14 cells of the half shell in the reference's filter order (mdrl_internal.h). */
 __constant__ int c_halfshell[kHalfShellCells][3] = MDRL_HALFSHELL_OFFSETS;
 
-/* Error bits raised by kernels and read by the host after a call. */
-enum : unsigned { kErrPosition = 1u, kErrType = 2u };
+/* Error bits raised by kernels and read by the host after a call.  kErrForce: a force sum that
+ * the accumulators cannot hold -- NaN or infinite, or (int64 fixed point) a magnitude at or above
+ * kFixMax, which the conversion would saturate. */
+enum : unsigned { kErrPosition = 1u, kErrType = 2u, kErrForce = 4u, kErrCellOverflow = 8u };
+
+/* Cell occupancy: cells up to kSortSmall particles are ordered in one shared-memory pass; larger
+ * ones in sorted chunks of kSortSmall merged by binary search; above kMaxCellOcc a cell raises
+ * kErrCellOverflow (MDRL_ERR_CELL_OVERFLOW), keeps its arrival order, and the force kernel skips
+ * the units that touch it, so a pathological input costs bounded time. */
+constexpr int kSortSmall = 1024;
+constexpr int kMaxCellOcc = 65536;
+
+/* The largest force (kcal/mol/A) a 2^-24 fixed-point component holds without saturating: the
+ * conversion clamps at 9e18 units. */
+constexpr float kFixMax = 9.0e18f / 16777216.0f;
 
 /* Per-type mass factors, kept in device memory and read through a pointer (a by-value kernel
  * parameter indexed by a particle's type would be copied to local memory in every thread). */
@@ -53,6 +79,16 @@ struct MassTab {
 
 __device__ __forceinline__ float wrap_d(float d, float L, float h) {
     return d > h ? __fsub_rn(d, L) : (d < -h ? __fadd_rn(d, L) : d);
+}
+
+/* The exact-difference rule per pair (MDRL_FLAG_EXACT_DIFF): the wrap direction from fl(xi - xj)
+ * as above, then the box edge comes off the high coordinate (exact for coordinates in [0, L):
+ * the one wrapped lies above L/2) and the difference is rounded once. */
+__device__ __forceinline__ float wrap_exact(float xi, float xj, float L, float h) {
+    const float d = __fsub_rn(xi, xj);
+    if (d > h) return __fsub_rn(__fsub_rn(xi, L), xj);
+    if (d < -h) return __fsub_rn(xi, __fsub_rn(xj, L));
+    return d;
 }
 
 template <bool SEP>
@@ -112,13 +148,14 @@ __device__ __forceinline__ void pair_functions(const TableDev &t, float r2, bool
             if (coul) { const float2 g = __ldg(t.e2 + 3 * idx + 2); v1 = madd<SEP>(g.y, r2e, g.x); }
         }
     } else {
-        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), r2e);
-        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), r2e);
-        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), r2e) : 0.0f;
+        const float x = table_variable(t, r2e);
+        v14 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx), x);
+        v8 = poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 1), x);
+        v3 = coul ? poly4<ORDER, SEP>(__ldg(t.f4 + 3 * idx + 2), x) : 0.0f;
         if (ENERGY) {
-            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), r2e);
-            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), r2e);
-            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), r2e) : 0.0f;
+            v12 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx), x);
+            v6 = poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 1), x);
+            v1 = coul ? poly4<ORDER, SEP>(__ldg(t.e4 + 3 * idx + 2), x) : 0.0f;
         }
     }
 }
@@ -142,11 +179,23 @@ __device__ __forceinline__ float combine_elj(float4 pc, float v12, float v6) {
                : __fmaf_rn(pc.z, v12, __fmul_rn(pc.w, v6));
 }
 
+/* 2^-24 fixed point.  NaN converts to 0 and magnitudes beyond kFixMax saturate; callers report
+ * both through force_ok / kErrForce rather than let them pass silently. */
 __device__ __forceinline__ unsigned long long to_fixed(float v) {
     float s = v * kFixScale;
     if (!(s == s)) s = 0.0f;
     s = fminf(fmaxf(s, -9.0e18f), 9.0e18f);
     return (unsigned long long)__float2ll_rn(s);
+}
+
+/* True when every component is finite and below kFixMax in magnitude (NaN fails the compare). */
+__device__ __forceinline__ bool force_ok(float fx, float fy, float fz) {
+    return fabsf(fx) < kFixMax && fabsf(fy) < kFixMax && fabsf(fz) < kFixMax;
+}
+
+/* Raise kErrForce when a force sum cannot be represented (one atomic per offending thread). */
+__device__ __forceinline__ void check_force(unsigned *err, float fx, float fy, float fz) {
+    if (!force_ok(fx, fy, fz) && err) atomicOr(err, kErrForce);
 }
 
 __device__ __forceinline__ float from_fixed(unsigned long long v) {
@@ -275,16 +324,25 @@ static __global__ void k_scatter(int n, const int *__restrict__ cell_of, const i
 }
 
 /* Order each cell's particles: by index (the reference's in-cell order, input order), or, when
- * key is given, by (key, index).  The rank of an element is the number of smaller ones. */
+ * key is given, by (key, index).  The rank of an element is the number of smaller ones (the
+ * (key, index) pairs are distinct).  scratch[n] (64-bit) holds the sorted chunks of cells above
+ * kSortSmall. */
 static __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict__ start,
                                                           const int *__restrict__ tmp,
                                                           int *__restrict__ sorted,
-                                                          const unsigned *__restrict__ key) {
-    __shared__ __align__(16) unsigned long long s_k[1024];
+                                                          const unsigned *__restrict__ key,
+                                                          unsigned long long *__restrict__ scratch,
+                                                          unsigned *__restrict__ err) {
+    __shared__ __align__(16) unsigned long long s_k[kSortSmall];
     const int c = blockIdx.x;
     const int s = start[c], m = start[c + 1] - s;
     if (m == 0) return;
-    if (m <= 1024) {
+    if (m > kMaxCellOcc) {
+        if (threadIdx.x == 0) atomicOr(err, kErrCellOverflow);
+        for (int e = threadIdx.x; e < m; e += blockDim.x) sorted[s + e] = tmp[s + e];
+        return;
+    }
+    if (m <= kSortSmall) {
         for (int e = threadIdx.x; e < m; e += blockDim.x) {
             const int id = tmp[s + e];
             s_k[e] = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id;
@@ -307,13 +365,38 @@ static __global__ void __launch_bounds__(128) k_cell_sort(const int *__restrict_
         }
         return;
     }
+    /* large cell: sort each chunk of kSortSmall in shared memory (rank count) into scratch ... */
+    for (int c0 = 0; c0 < m; c0 += kSortSmall) {
+        const int mc = min(kSortSmall, m - c0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < mc; e += blockDim.x) {
+            const int id = tmp[s + c0 + e];
+            s_k[e] = ((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < mc; e += blockDim.x) {
+            const unsigned long long me = s_k[e];
+            int r = 0;
+            for (int q = 0; q < mc; ++q) r += s_k[q] < me;
+            scratch[s + c0 + r] = me;
+        }
+    }
+    __syncthreads();   /* the block's global writes are visible to the block after the barrier */
+    /* ... then an element's rank = its rank in its chunk + the keys below it in every other chunk
+     * (binary search: O(m log kSortSmall / kSortSmall) per element) */
     for (int e = threadIdx.x; e < m; e += blockDim.x) {
-        const int ide = tmp[s + e];
-        const unsigned long long me = ((unsigned long long)(key ? key[ide] : 0u) << 32) | (unsigned)ide;
-        int r = 0;
-        for (int q = 0; q < m; ++q) {
-            const int id = tmp[s + q];
-            r += (((unsigned long long)(key ? key[id] : 0u) << 32) | (unsigned)id) < me;
+        const unsigned long long me = scratch[s + e];
+        const int ce = e / kSortSmall;
+        int r = e - ce * kSortSmall;
+        for (int c0 = 0, cc = 0; c0 < m; c0 += kSortSmall, ++cc) {
+            if (cc == ce) continue;
+            const unsigned long long *a = scratch + s + c0;
+            int lo = 0, hi = min(kSortSmall, m - c0);   /* first index with a[idx] >= me */
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (a[mid] < me) lo = mid + 1; else hi = mid;
+            }
+            r += lo;
         }
         sorted[s + r] = (int)(me & 0xffffffffu);
     }
@@ -574,14 +657,21 @@ template <int ORDER, bool SEP>
 static __global__ void k_pair_eval(int n, const float4 *__restrict__ ref, const float4 *__restrict__ nbr,
                             const int *__restrict__ tref, const int *__restrict__ tnbr, Geom g,
                             TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke,
-                            float4 *__restrict__ out, float2 *__restrict__ aux) {
+                            float4 *__restrict__ out, float2 *__restrict__ aux, int exact) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const float4 a = ref[k], b = nbr[k];
     const int ta = tref ? tref[k] : 0, tb = tnbr ? tnbr[k] : 0;
-    const float dx = wrap_d(__fsub_rn(a.x, b.x), g.L[0], g.h[0]);
-    const float dy = wrap_d(__fsub_rn(a.y, b.y), g.L[1], g.h[1]);
-    const float dz = wrap_d(__fsub_rn(a.z, b.z), g.L[2], g.h[2]);
+    float dx, dy, dz;
+    if (exact) {
+        dx = wrap_exact(a.x, b.x, g.L[0], g.h[0]);
+        dy = wrap_exact(a.y, b.y, g.L[1], g.h[1]);
+        dz = wrap_exact(a.z, b.z, g.L[2], g.h[2]);
+    } else {
+        dx = wrap_d(__fsub_rn(a.x, b.x), g.L[0], g.h[0]);
+        dy = wrap_d(__fsub_rn(a.y, b.y), g.L[1], g.h[1]);
+        dz = wrap_d(__fsub_rn(a.z, b.z), g.L[2], g.h[2]);
+    }
     const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
     float fs = 0.0f;

@@ -182,7 +182,7 @@ __global__ void k_pme_convolve(int ncplx, int K2h, int K2, cufftComplex *__restr
 
 template <int P, int ACC>
 __global__ void k_pme_gather(int n, const float4 *__restrict__ pos, PmeGeom pg, const float *__restrict__ phi,
-                             unsigned long long *__restrict__ F64, float *__restrict__ F32) {
+                             unsigned long long *__restrict__ F64, float *__restrict__ F32, unsigned *__restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 r = pos[i];
@@ -217,11 +217,13 @@ __global__ void k_pme_gather(int n, const float4 *__restrict__ pos, PmeGeom pg, 
     fy *= -r.w * pg.scale[1];
     fz *= -r.w * pg.scale[2];
     if (ACC == MDRL_ACC_FIXED64) {
+        check_force(err, fx, fy, fz);
         F64[i] += to_fixed(fx);
         F64[(size_t)n + i] += to_fixed(fy);
         F64[2 * (size_t)n + i] += to_fixed(fz);
     } else {
         /* the high planes; with compensation the low planes take the rounding of the add */
+        if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(err, kErrForce);
         const float add[3] = {fx, fy, fz};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -420,13 +422,13 @@ mdrl_status pme_enqueue(mdrl_ctx *c, int n, const float4 *pos, unsigned long lon
     PME_FFT(cufftExecC2R(s->bwd, s->d_cplx, s->d_real));
     const int acc = c->p.accum;
     if (s->p.order == 6) {
-        if (acc == MDRL_ACC_FIXED64) k_pme_gather<6, MDRL_ACC_FIXED64><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
-        else if (acc == MDRL_ACC_KAHAN) k_pme_gather<6, MDRL_ACC_KAHAN><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
-        else k_pme_gather<6, MDRL_ACC_FP32_ATOMIC><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
+        if (acc == MDRL_ACC_FIXED64) k_pme_gather<6, MDRL_ACC_FIXED64><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
+        else if (acc == MDRL_ACC_KAHAN) k_pme_gather<6, MDRL_ACC_KAHAN><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
+        else k_pme_gather<6, MDRL_ACC_FP32_ATOMIC><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
     } else {
-        if (acc == MDRL_ACC_FIXED64) k_pme_gather<4, MDRL_ACC_FIXED64><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
-        else if (acc == MDRL_ACC_KAHAN) k_pme_gather<4, MDRL_ACC_KAHAN><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
-        else k_pme_gather<4, MDRL_ACC_FP32_ATOMIC><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32);
+        if (acc == MDRL_ACC_FIXED64) k_pme_gather<4, MDRL_ACC_FIXED64><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
+        else if (acc == MDRL_ACC_KAHAN) k_pme_gather<4, MDRL_ACC_KAHAN><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
+        else k_pme_gather<4, MDRL_ACC_FP32_ATOMIC><<<qb, 256, 0, c->stream>>>(n, pos, pg, s->d_real, F64, F32, c->d_err);
     }
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;

@@ -17,14 +17,19 @@
  * Limits: n <= 131,072 particles, <= 4,096 cells, nseg * bins <= 16,384 table entries, int64
  * fixed-point accumulation only; larger requests are rejected with MDRL_ERR_RANGE and a message.
  *
- * Set-up: the first call on a device (with that device current) looks up the device address of
- * the array with cudaGetSymbolAddress; make that first call before any stream capture.  Tables
- * are fitted on the host and copied into the array when the table parameters change.
+ * Set-up: every call looks up the device address of the array in the current CUDA context with
+ * cudaGetSymbolAddress (a __device__ array has one copy per context, so an address cached from
+ * another context, or from before a cudaDeviceReset, would be stale).  Tables are fitted on the
+ * host and copied into the array when the table parameters change or the array belongs to a
+ * context (unique context ID) or address other than the one the copy went to; the first call in
+ * a context therefore copies tables, so make it before any stream capture.  The call runs on the
+ * current device, which must be p->device.
  *
  * Sharing: every call uses the same array, which keeps the previous call's contents; the call
  * clears what must start at zero.  Two calls whose work overlaps on the GPU (different streams,
  * or threads without ordering) race on the array: serialise them.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -51,7 +56,7 @@ constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 /* Byte offsets of the sub-buffers inside the array. */
 struct Layout {
-    size_t err, tot, count, start, unit, cell_of, slot, tmp, sorted, key, pos, type, id, F64, tabf,
+    size_t err, tot, count, start, unit, cell_of, slot, tmp, sorted, key, sortkey, pos, type, id, F64, tabf,
         tabe, tabr, pcoef, end;
 };
 
@@ -68,6 +73,7 @@ constexpr Layout make_layout() {
     l.tmp = o;     o = align256(o + sizeof(int) * kStaticMaxN);
     l.sorted = o;  o = align256(o + sizeof(int) * kStaticMaxN);
     l.key = o;     o = align256(o + sizeof(unsigned) * kStaticMaxN);
+    l.sortkey = o; o = align256(o + sizeof(unsigned long long) * kStaticMaxN);
     l.pos = o;     o = align256(o + sizeof(float4) * kStaticMaxN);
     l.type = o;    o = align256(o + sizeof(int) * kStaticMaxN);
     l.id = o;      o = align256(o + sizeof(int) * kStaticMaxN);
@@ -83,9 +89,11 @@ constexpr Layout make_layout() {
 constexpr Layout kLayout = make_layout();
 static_assert(kLayout.end <= kStaticBytes, "static scratch layout exceeds the array");
 
-/* What the array currently holds on one device. */
+/* Which tables the array holds on one device: valid only for the context (unique ID) and
+ * array address they were copied to. */
 struct DeviceSlot {
-    unsigned char *base = nullptr;   /* device address of g_static_scratch */
+    unsigned long long ctx_id = 0;   /* 0: unknown context, never matches */
+    unsigned char *base = nullptr;   /* device address of g_static_scratch the tables went to */
     bool have_tables = false;
     int order = 0, nseg = 0, bins = 0, min_log2 = 0, ntypes = 0;
     double sigma[MDRL_MAX_TYPES] = {}, epsilon[MDRL_MAX_TYPES] = {};
@@ -94,6 +102,37 @@ struct DeviceSlot {
 std::mutex g_mu;
 DeviceSlot g_slots[kStaticMaxDevices];
 
+/* The unique ID of the current CUDA context (cuCtxGetCurrent + cuCtxGetId through the runtime's
+ * driver entry points, so the library needs no link-time dependency on the driver library), or
+ * 0 when it cannot be obtained, in which case the tables are copied on every call. */
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
+
+unsigned long long current_context_id() {
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = (ctx_get_current_fn)f1;
+            get_id = (ctx_get_id_fn)f2;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
 mdrl_status fail(mdrl_status s, const std::string &msg) {
     set_error("mdrl_force_eval_static: " + msg);
     return s;
@@ -101,6 +140,7 @@ mdrl_status fail(mdrl_status s, const std::string &msg) {
 
 #define ST_CUDA(call)                                                                             \
     do {                                                                                          \
+        if (fault_hit(#call)) return fail(MDRL_ERR_CUDA, std::string(#call) + ": injected failure (MDRL_FAULT)"); \
         cudaError_t e_ = (call);                                                                  \
         if (e_ != cudaSuccess) return fail(MDRL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
@@ -121,18 +161,15 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
                                               float *fy, float *fz, int64_t *pairs_out, void *stream_ptr) {
     if (!p || n < 0 || (n > 0 && (!x || !y || !z || !fx || !fy || !fz)))
         return fail(MDRL_ERR_INVALID_ARG, "null or invalid argument");
+    fault_arm_from_env(false);
     if (n > kStaticMaxN)
         return fail(MDRL_ERR_RANGE, "n = " + std::to_string(n) + " exceeds the static scratch limit of " +
                                         std::to_string(kStaticMaxN) + " particles");
     if (p->accum != MDRL_ACC_FIXED64)
         return fail(MDRL_ERR_INVALID_ARG, "only int64 fixed-point accumulation (MDRL_ACC_FIXED64) is supported");
-    if (p->ntypes < 1 || p->ntypes > MDRL_MAX_TYPES || p->table_order < 1 || p->table_order > 3 ||
-        p->table_bins < 16 || p->table_bins > 4096 || (p->table_bins & (p->table_bins - 1)) ||
-        !(p->cutoff > 0.0) || (p->eval != MDRL_EVAL_TABLE && p->eval != MDRL_EVAL_DIRECT) ||
-        (p->arith != MDRL_ARITH_FMA && p->arith != MDRL_ARITH_SEPARATE))
-        return fail(MDRL_ERR_INVALID_ARG, "invalid parameters");
-    for (int t = 0; t < p->ntypes; ++t)
-        if (!(p->sigma[t] > 0) || !(p->epsilon[t] >= 0)) return fail(MDRL_ERR_INVALID_ARG, "invalid type parameters");
+    /* the checks mdrl_create makes (box, cutoff, types, table parameters incl. the first segment's
+     * exponent, modes, coulomb_k) */
+    if (validate_params(p) != MDRL_OK) return fail(MDRL_ERR_INVALID_ARG, mdrl_last_error());
 
     /* geometry, as mdrl_create sets it up */
     Geom g;
@@ -142,7 +179,10 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     for (int d = 0; d < 3; ++d) {
         if (!(p->box[d] > 0.0)) return fail(MDRL_ERR_INVALID_ARG, "box edges must be positive");
         const float L = (float)p->box[d];
-        const int nc = p->ncell[d] > 0 ? p->ncell[d] : (int)std::floor((double)L / (double)rcf);
+        const double ncd = p->ncell[d] > 0 ? (double)p->ncell[d] : std::floor((double)L / (double)rcf);
+        if (ncd > (double)kStaticMaxCells)
+            return fail(MDRL_ERR_RANGE, "axis " + std::to_string(d) + ": more cells than the static scratch holds");
+        const int nc = (int)ncd;
         g.L[d] = L;
         g.h[d] = 0.5f * L;
         g.nc[d] = nc;
@@ -157,24 +197,27 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     const int order = p->table_order, bins = p->table_bins, m0 = p->table_min_log2;
     const int nseg = seg_count(g.rc2, m0);
     if (nseg < 1) return fail(MDRL_ERR_RANGE, "cutoff lies below the first table segment");
-    const int nidx = nseg * bins;
-    if (nidx > kStaticMaxTable)
-        return fail(MDRL_ERR_RANGE, std::to_string(nidx) + " table entries exceed the static scratch limit of " +
+    const long long nidx64 = (long long)nseg * bins;   /* 64-bit: no overflow before the check */
+    if (nidx64 > kStaticMaxTable)
+        return fail(MDRL_ERR_RANGE, std::to_string(nidx64) + " table entries exceed the static scratch limit of " +
                                         std::to_string(kStaticMaxTable));
+    const int nidx = (int)nidx64;
 
     int dev = 0;
     ST_CUDA(cudaGetDevice(&dev));
+    if (dev != p->device)
+        return fail(MDRL_ERR_INVALID_ARG, "p->device (" + std::to_string(p->device) +
+                                              ") is not the current device (" + std::to_string(dev) + ")");
     if (dev < 0 || dev >= kStaticMaxDevices) return fail(MDRL_ERR_RANGE, "device ordinal too large");
     cudaStream_t st = (cudaStream_t)stream_ptr;
 
     std::lock_guard<std::mutex> lock(g_mu);
     DeviceSlot &slot = g_slots[dev];
-    if (!slot.base) {
-        void *ptr = nullptr;
-        ST_CUDA(cudaGetSymbolAddress(&ptr, g_static_scratch));
-        slot.base = (unsigned char *)ptr;
-    }
-    unsigned char *b = slot.base;
+    /* the array's address in the current context, looked up on every call */
+    void *ptr = nullptr;
+    ST_CUDA(cudaGetSymbolAddress(&ptr, g_static_scratch));
+    unsigned char *b = (unsigned char *)ptr;
+    const unsigned long long ctx_id = current_context_id();
     unsigned *d_err = (unsigned *)(b + kLayout.err);
     DevTotals *d_tot = (DevTotals *)(b + kLayout.tot);
     int *d_count = (int *)(b + kLayout.count);
@@ -185,6 +228,7 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     int *d_tmp = (int *)(b + kLayout.tmp);
     int *d_sorted = (int *)(b + kLayout.sorted);
     unsigned *d_key = (unsigned *)(b + kLayout.key);
+    unsigned long long *d_sortkey = (unsigned long long *)(b + kLayout.sortkey);
     float4 *d_pos = (float4 *)(b + kLayout.pos);
     int *d_type = (int *)(b + kLayout.type);
     int *d_id = (int *)(b + kLayout.id);
@@ -192,13 +236,16 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     float4 *d_pcoef = (float4 *)(b + kLayout.pcoef);
 
     /* tables and multipliers: refit and copy in when they differ from what the array holds */
-    bool same = slot.have_tables && slot.order == order && slot.nseg == nseg && slot.bins == bins &&
-                slot.min_log2 == m0 && slot.ntypes == p->ntypes;
+    bool same = slot.have_tables && ctx_id != 0 && slot.ctx_id == ctx_id && slot.base == b &&
+                slot.order == order && slot.nseg == nseg && slot.bins == bins && slot.min_log2 == m0 &&
+                slot.ntypes == p->ntypes;
     for (int t = 0; same && t < p->ntypes; ++t)
         same = slot.sigma[t] == p->sigma[t] && slot.epsilon[t] == p->epsilon[t];
     if (!same) {
+        /* the copies below overwrite the array: it holds no valid tables until they complete */
+        slot.have_tables = false;
         std::vector<float> tab;
-        fit_tables(order, nseg, bins, m0, 8, &tab);
+        fit_tables(order, nseg, bins, m0, 8, &tab, 0.0, order >= 2);
         std::vector<float> pc;
         mix_pair_coefficients(*p, &pc, nullptr);
         const int nc = order + 1;
@@ -235,6 +282,8 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
         ST_CUDA(cudaMemcpyAsync(d_pcoef, pc4.data(), sizeof(float4) * pc4.size(), cudaMemcpyHostToDevice, st));
         ST_CUDA(cudaStreamSynchronize(st)); /* the host vectors go out of scope */
         slot.have_tables = true;
+        slot.ctx_id = ctx_id;
+        slot.base = b;
         slot.order = order; slot.nseg = nseg; slot.bins = bins; slot.min_log2 = m0; slot.ntypes = T;
         for (int t = 0; t < T; ++t) { slot.sigma[t] = p->sigma[t]; slot.epsilon[t] = p->epsilon[t]; }
     }
@@ -246,6 +295,7 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     int lb = 0;
     while ((1 << lb) < bins) ++lb;
     tab.lb = lb; tab.min_log2 = m0; tab.r2min = std::ldexp(1.0f, m0);
+    tab.local = order >= 2 ? 1 : 0;   /* as a context fits them */
 
     /* state that must start at zero; the previous call's contents are otherwise left in place */
     const int nc = (int)ncells;
@@ -257,18 +307,19 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     k_scan<<<1, 1024, 0, st>>>(nc, d_count, d_start, d_tot);
     if (n > 0) {
         k_scatter<<<grid, blk, 0, st>>>(n, d_cell_of, d_slot, d_start, d_tmp);
-        k_cell_sort<<<nc, 128, 0, st>>>(d_start, d_tmp, d_sorted, d_key);
+        k_cell_sort<<<nc, 128, 0, st>>>(d_start, d_tmp, d_sorted, d_key, d_sortkey, d_err);
         k_gather_user<<<grid, blk, 0, st>>>(n, d_sorted, x, y, z, q, type, d_pos, d_type, d_id, d_F64, nullptr,
                                             nullptr, p->ntypes, d_err);
     }
     const int ord = p->eval == MDRL_EVAL_DIRECT ? 0 : order;
-    force_fn fn = pick_force(ord, p->arith == MDRL_ARITH_SEPARATE, false, MDRL_ACC_FIXED64);
+    force_fn fn = pick_force(ord, p->arith == MDRL_ARITH_SEPARATE, false, MDRL_ACC_FIXED64, kFW, false,
+                             (p->flags & MDRL_FLAG_EXACT_DIFF) != 0);
     const size_t smem = force_smem_bytes(p->ntypes, false);
     ST_CUDA(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)force_smem_bytes(MDRL_MAX_TYPES, true, 8)));
     fn<<<nc * kHalfShellCells, kFT, smem, st>>>(d_pos, d_type, d_start, g, tab, d_pcoef, p->ntypes,
                                                 (float)p->coulomb_k, n, d_F64, nullptr, nullptr, d_unit, nullptr,
-                                                nullptr, tile_word(kStepsPerPiece, 0));
+                                                nullptr, tile_word(kStepsPerPiece, 0), d_err);
     k_totals<<<1, 1024, 0, st>>>(force_items(nc), d_unit, 0, nullptr, d_tot, 0);
     if (n > 0)
         k_unsort<<<grid, blk, 0, st>>>(n, d_id, d_F64, nullptr, nullptr, fx, fy, fz, nullptr);
@@ -278,8 +329,8 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     ST_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     ST_CUDA(cudaMemcpyAsync(&tot, d_tot, sizeof(DevTotals), cudaMemcpyDeviceToHost, st));
     ST_CUDA(cudaStreamSynchronize(st));
-    if (err & kErrPosition) return fail(MDRL_ERR_INVALID_ARG, "positions must be finite and lie in [0, box)");
-    if (err & kErrType) return fail(MDRL_ERR_INVALID_ARG, "particle types must lie in [0, ntypes)");
+    const mdrl_status es = device_error_status(err);
+    if (es != MDRL_OK) return fail(es, mdrl_last_error());
     if (pairs_out) *pairs_out = (int64_t)tot.pairs;
     return MDRL_OK;
 }

@@ -28,6 +28,13 @@ namespace mdrl {
 
 static const double kExponent[kNumFunc] = {-7.0, -4.0, -1.5, -6.0, -3.0, -0.5};
 
+/* log2 of a power of two (the bin widths 2^(min_log2 + s) / bins). */
+static int ilog2_exact(double w) {
+    int e;
+    std::frexp(w, &e);
+    return e - 1;
+}
+
 /* Least-squares fit of degree `order` to (t_i, y_i), i < m, by Householder QR.  Returns
  * coefficients a[0..order] of a0 + a1 t + ... */
 static void lsq_fit(int m, int order, const double *t, const double *y, double *a) {
@@ -80,7 +87,8 @@ static double unit_function(int f, double x, double beta) {
     return std::pow(x, kExponent[f]);
 }
 
-void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out, double beta) {
+void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::vector<float> *out, double beta,
+                bool local) {
     const int nidx = nseg * bins;
     const int nc = order + 1;
     out->assign((size_t)kNumFunc * nc * nidx, 0.0f);
@@ -96,6 +104,14 @@ void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::v
                     y[i] = unit_function(f, x0 + t[i] * width, beta);
                 }
                 lsq_fit(samples, order, t.data(), y.data(), a.data());
+                const int idx = s * bins + j;
+                if (local) {
+                    /* p = sum_m a_m (u / w)^m with u = x - x0: coefficients a_m / w^m (w is a
+                     * power of two, so the scaling is exact) */
+                    for (int m = 0; m < nc; ++m)
+                        (*out)[((size_t)f * nc + m) * nidx + idx] = (float)std::ldexp(a[m], -m * ilog2_exact(width));
+                    continue;
+                }
                 /* p(x) = sum_m a_m ((x - x0)/w)^m  ->  sum_k c_k x^k */
                 for (int k = 0; k < nc; ++k) c[k] = 0.0;
                 for (int m = 0; m < nc; ++m) {
@@ -106,7 +122,6 @@ void fit_tables(int order, int nseg, int bins, int min_log2, int samples, std::v
                         binom = binom * (m - k) / (k + 1);
                     }
                 }
-                const int idx = s * bins + j;
                 for (int k = 0; k < nc; ++k)
                     (*out)[((size_t)f * nc + k) * nidx + idx] = (float)c[k];
             }

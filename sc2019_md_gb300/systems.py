@@ -45,6 +45,10 @@ class System:
     epsilon: list
     mass: list
     coulomb_k: float
+    # first table point r2 = 2^table_min_log2: the square of the workload's minimum separation
+    # (rounded down to a power of two), so that pairs pushed closer during MD are evaluated at a
+    # finite, representable force instead of the far larger one at the library default 2^-2
+    table_min_log2: int = -2
 
     @property
     def n(self) -> int:
@@ -55,7 +59,7 @@ class System:
         T = len(self.sigma)
         p = default_params(box=self.box, cutoff=self.cutoff, ncell=self.ncell, ntypes=T,
                            sigma=self.sigma, epsilon=self.epsilon, mass=self.mass,
-                           coulomb_k=self.coulomb_k)
+                           coulomb_k=self.coulomb_k, table_min_log2=self.table_min_log2)
         for k, v in kw.items():
             setattr(p, k, v)
         return p
@@ -108,7 +112,7 @@ def lj1728(seed_offset: int = 0) -> System:
     pos = wrap_into_box(pos, (L, L, L))
     m = np.full(len(pos), 39.95)
     return System("lj1728", (L, L, L), 8.5, (3, 3, 3), pos, maxwell(len(pos), m, 300.0, rng),
-                  None, np.zeros(len(pos), np.int32), [3.4], [0.238], [39.95], 0.0)
+                  None, np.zeros(len(pos), np.int32), [3.4], [0.238], [39.95], 0.0, table_min_log2=0)
 
 
 def ljc92k(n: int = 92224, box=(108.86, 108.86, 77.76), seed_offset: int = 0) -> System:
@@ -124,7 +128,7 @@ def ljc92k(n: int = 92224, box=(108.86, 108.86, 77.76), seed_offset: int = 0) ->
     m = np.asarray(mass)[t]
     ncell = tuple(int(np.floor(np.float32(b) / np.float32(12.0))) for b in box)
     return System("ljc92k", tuple(box), 12.0, ncell, pos, maxwell(n, m, 300.0, rng),
-                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K, table_min_log2=0)
 
 
 def ljc1m(n: int = 1048576, L: float = 224.0, seed_offset: int = 0) -> System:
@@ -140,7 +144,7 @@ def ljc1m(n: int = 1048576, L: float = 224.0, seed_offset: int = 0) -> System:
     m = np.asarray(mass)[t]
     nc = int(np.floor(np.float32(L) / np.float32(10.0)))
     return System("ljc1m", (L, L, L), 10.0, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
-                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K, table_min_log2=0)
 
 
 def small_ljc(n: int, L: float, cutoff: float, seed: int, ntypes: int = 4,
@@ -157,7 +161,8 @@ def small_ljc(n: int, L: float, cutoff: float, seed: int, ntypes: int = 4,
     m = np.asarray(mass)[t]
     nc = int(np.floor(np.float32(L) / np.float32(cutoff)))
     return System("small_ljc", box, cutoff, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
-                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K)
+                  q.astype(np.float32), t, sigma, eps, mass, COULOMB_K,
+                  table_min_log2=int(np.floor(np.log2(dmin * dmin))) if dmin > 0 else -2)
 
 
 def replica(n: int, r: int, density: float = 0.1, cutoff: float = 10.0, dmin: float = 1.0) -> System:
@@ -175,7 +180,8 @@ def replica(n: int, r: int, density: float = 0.1, cutoff: float = 10.0, dmin: fl
     m = np.full(n, 39.95)
     nc = max(1, int(np.floor(np.float32(L) / np.float32(cutoff))))
     return System(f"replica{r}", box, cutoff, (nc, nc, nc), pos, maxwell(n, m, 300.0, rng),
-                  q.astype(np.float32), np.zeros(n, np.int32), [3.4], [0.238], [39.95], COULOMB_K)
+                  q.astype(np.float32), np.zeros(n, np.int32), [3.4], [0.238], [39.95], COULOMB_K,
+                  table_min_log2=int(np.floor(np.log2(dmin * dmin))) if dmin > 0 else -2)
 
 
 def batch_sizes(count: int = 512, lo: int = 500, hi: int = 20000) -> np.ndarray:

@@ -44,7 +44,24 @@ def oracle_from_ctx(ctx: m.Context, sysm, arith=None, eval_mode=None):
     return oracle.System(sysm.pos, sysm.box, sysm.ncell, sysm.cutoff, pc, q=sysm.q, type=sysm.type,
                          ke=p.coulomb_k, tab=tab, order=meta["order"], nseg=meta["nseg"], bins=meta["bins"],
                          min_log2=meta["min_log2"], eval=p.eval if eval_mode is None else eval_mode,
-                         arith=p.arith if arith is None else arith, pcoef64=pc64, ke64=p.coulomb_k)
+                         arith=p.arith if arith is None else arith, pcoef64=pc64, ke64=p.coulomb_k,
+                         local=meta["local"], exact=bool(p.flags & m.FLAG_EXACT_DIFF))
+
+
+def liquid_argon(seed: int = 3):
+    """A liquid-argon state point (1,728 atoms in a 36 A box, 120 K, rc 8.5 A, 4x4x4 cells): a
+    jittered lattice that melts without exploding, for energy-conservation checks."""
+    from sc2019_md_gb300 import systems
+    rng = np.random.default_rng(seed)
+    L = 36.0
+    nside = 12
+    g = (np.arange(nside) + 0.5) * (L / nside)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1) + rng.uniform(-0.05, 0.05, (nside ** 3, 3))
+    pos = systems.wrap_into_box(pos, (L, L, L))
+    vel = systems.maxwell(len(pos), np.full(len(pos), 39.95), 120.0, rng)
+    return systems.System("argon", (L, L, L), 8.5, (4, 4, 4), pos, vel, None, np.zeros(len(pos), np.int32),
+                          [3.4], [0.238], [39.95], 0.0)
 
 
 def force_err(F, Fref):

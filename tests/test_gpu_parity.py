@@ -38,15 +38,17 @@ def test_pair_eval_kat1_bit_exact():
 
 
 @pytest.mark.parametrize("order,bins", [(0, 256), (1, 256), (1, 512), (2, 256), (3, 256)])
-@pytest.mark.parametrize("arith", [m.ARITH_FMA, m.ARITH_SEPARATE])
-def test_pair_eval_random_vs_oracle(order, bins, arith):
-    """Random periodic pairs of 4 types with charges: bit-identical to the oracle's datapath."""
+@pytest.mark.parametrize("arith,exact", [(m.ARITH_FMA, False), (m.ARITH_SEPARATE, False), (m.ARITH_FMA, True)])
+def test_pair_eval_random_vs_oracle(order, bins, arith, exact):
+    """Random periodic pairs of 4 types with charges: bit-identical to the oracle's datapath (both
+    difference rules; orders 2-3 with the library's bin-local tables)."""
     rng = np.random.default_rng(100 + order * 7 + arith)
     n = 4000
     L = 40.0
     sysm = systems.small_ljc(64, L, 12.0, seed=3)
     p = sysm.params(table_order=max(order, 1), table_bins=bins, arith=arith,
-                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE)
+                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE,
+                    flags=m.FLAG_EXACT_DIFF if exact else 0)
     a = rng.uniform(0, L, (n, 3)).astype(np.float32)
     b = (a + rng.uniform(-13, 13, (n, 3))).astype(np.float32) % np.float32(L)
     b[:50] = a[:50]                                   # r2 = 0 pairs are filtered
@@ -107,13 +109,31 @@ def _check_force(sysm, params, tol=SUM_TOL, tile=None):
     return F, Fo, o
 
 
-@pytest.mark.parametrize("order,bins", [(0, 256), (1, 256), (1, 512), (2, 256)])
-@pytest.mark.parametrize("arith", [m.ARITH_FMA, m.ARITH_SEPARATE])
-def test_force_small_ljc(order, bins, arith):
+@pytest.mark.parametrize("order,bins", [(0, 256), (1, 256), (1, 512), (2, 256), (3, 128)])
+@pytest.mark.parametrize("arith,exact", [(m.ARITH_FMA, False), (m.ARITH_SEPARATE, False), (m.ARITH_FMA, True)])
+def test_force_small_ljc(order, bins, arith, exact):
     sysm = systems.small_ljc(3000, 37.5, 12.0, seed=21)          # 3x3x3 cells, ~110 per cell
     p = sysm.params(table_order=max(order, 1), table_bins=bins, arith=arith,
-                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE, flags=m.FLAG_ENERGY)
+                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE,
+                    flags=m.FLAG_ENERGY | (m.FLAG_EXACT_DIFF if exact else 0))
     _check_force(sysm, p)
+
+
+@pytest.mark.parametrize("accum", [m.ACC_FIXED64, m.ACC_FP32_ATOMIC])
+@pytest.mark.parametrize("which", ["lj1728", "ljc92k"])
+def test_force_error_bound(which, accum):
+    """The stated accuracy: with the exact-difference rule and the library's bin-local order-2
+    tables (512 bins), the GPU forces are within 1e-5 of the FP64 direct oracle in the primary
+    norm, max_i |dF_i| / rms_j |F_j| (median per-particle relative error within 1e-6), for the
+    fixed-point ("tuned") and the FP32-atomic ("plain") accumulation alike; partner counts
+    bit-equal to the oracle's exact-rule datapath."""
+    sysm = getattr(systems, which)()
+    p = sysm.params(table_order=2, table_bins=512, flags=m.FLAG_EXACT_DIFF, accum=accum)
+    F, Fo, o = _check_force(sysm, p)
+    F64, _ = o.force_direct64()
+    emax, emed = force_err(F, F64)
+    assert emax <= 1e-5, emax
+    assert emed <= 1e-6, emed
 
 
 def test_force_lj1728_and_fp64_error():
@@ -221,12 +241,14 @@ def test_cutoff_boundary_pairs(ncell, L, ndimers, seed, tile):
 
 
 @pytest.mark.parametrize("tile", [None, (4, 6, 1), (8, 4, 1)])
-def test_full_size_ljc92k_counts_and_forces(tile):
+@pytest.mark.parametrize("exact", [False, True])
+def test_full_size_ljc92k_counts_and_forces(tile, exact):
     """The 92,224-atom LJ+Coulomb system at full size, with the default tile and with pruned
-    (survivor-list) tiles: partner counts and pair total bit-equal to the oracle, forces within the
-    summation tolerance."""
+    (survivor-list) tiles, the reference's difference rule (order-1 tables) and the exact rule
+    (bin-local order-2 tables): partner counts and pair total bit-equal to the oracle, forces within
+    the summation tolerance."""
     sysm = systems.ljc92k()
-    p = sysm.params(table_bins=512)
+    p = sysm.params(table_bins=512, table_order=2 if exact else 1, flags=m.FLAG_EXACT_DIFF if exact else 0)
     F, Fo, o = _check_force(sysm, p, tile=tile)
 
 

@@ -1,8 +1,11 @@
-"""The precision sweep on the 1,728-atom LJ argon system: force accumulation {int64 fixed point,
-FP32 atomics, compensated FP32} x evaluation {direct FP32, 1st-order, 2nd-order tables} x
-{64, 256, 1024} bins.  For each variant: per-particle force error against the FP64 direct oracle
-(both norms), run-to-run bit reproducibility, and the NVE energy drift (linear-fit slope of the
-total energy) over 10,000 velocity-Verlet steps of 2 fs.  With MDRL_REPORT_DIR set the table is
+"""The precision sweep: force accumulation {int64 fixed point, FP32 atomics, compensated FP32} x
+evaluation {direct FP32, 1st-order, 2nd-order tables} x {64, 256, 1024} bins.  For each variant:
+per-particle force error against the FP64 direct oracle on the 1,728-atom system (both norms),
+run-to-run bit reproducibility, and the NVE energy drift (linear-fit slope of the total energy)
+over 10,000 velocity-Verlet steps of 2 fs on two systems: the 1,728-atom cube, whose sigma-3.4 A
+atoms 2.1 A apart explode (its row records the step at which a force sum left what the
+accumulators hold, or the slope if it never did), and a liquid-argon state that conserves energy,
+where the drift measures the accumulation and the tables.  With MDRL_REPORT_DIR set the table is
 written there as precision_sweep.json."""
 import json
 import os
@@ -12,52 +15,83 @@ import pytest
 
 import sc2019_md_gb300 as m
 from sc2019_md_gb300 import systems
-from helpers import force_err, oracle_from_ctx
+from helpers import force_err, liquid_argon, oracle_from_ctx
 
 pytestmark = pytest.mark.gpu
 
 ACC = {"fixed64": m.ACC_FIXED64, "fp32_atomic": m.ACC_FP32_ATOMIC, "kahan_fp32": m.ACC_KAHAN}
 EVALS = [("direct", 0, 256)] + [(f"order{o}", o, b) for o in (1, 2) for b in (64, 256, 1024)]
+STEPS, CHUNK, DT = 10000, 100, 2.0
 
 
-def _variant(sysm, acc, order, bins):
-    p = sysm.params(accum=ACC[acc], table_order=max(order, 1), table_bins=bins,
-                    eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE, flags=m.FLAG_ENERGY)
+def _params(sysm, acc, order, bins, exact=False):
+    return sysm.params(accum=ACC[acc], table_order=max(order, 1), table_bins=bins,
+                       eval=m.EVAL_DIRECT if order == 0 else m.EVAL_TABLE,
+                       flags=m.FLAG_ENERGY | (m.FLAG_EXACT_DIFF if exact else 0))
+
+
+def _nve(p, sysm):
+    """Total energy every CHUNK steps over STEPS steps: (slope kcal/mol/ps or None, mean KE, the
+    step at which MDRL_ERR_RANGE stopped the run or None)."""
+    x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
+    energies, kin = [], []
+    with m.Context(p) as ctx:
+        try:
+            ctx.set_state(x, y, z, sysm.vel, sysm.q, sysm.type)
+            for k in range(STEPS // CHUNK):
+                st = ctx.step(CHUNK)
+                energies.append(st["e_lj"] + st["e_coul"] + st["kinetic"])
+                kin.append(st["kinetic"])
+        except m.MdrlError as e:
+            assert e.status == 3, e                     # forces beyond the accumulators: reported
+            return None, None, len(energies) * CHUNK
+    e = np.asarray(energies)
+    t = np.arange(len(e)) * CHUNK * DT * 1e-3                        # ps
+    return float(np.polyfit(t, e, 1)[0]), float(np.mean(kin)), None
+
+
+def _variant(sysm, liq, acc, order, bins, exact=False):
+    p = _params(sysm, acc, order, bins, exact)
     x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
     with m.Context(p) as ctx:
         F1, _, _ = ctx.force(x, y, z, None, sysm.type)
         F2, _, _ = ctx.force(x, y, z, None, sysm.type)
         o = oracle_from_ctx(ctx, sysm)
-        ctx.set_state(x, y, z, sysm.vel, None, sysm.type)
-        energies = []
-        for _ in range(100):
-            st = ctx.step(100)
-            energies.append(st["e_lj"] + st["kinetic"])
     F64, _ = o.force_direct64()
     emax, emed = force_err(F1, F64)
-    e = np.asarray(energies)
-    t = np.arange(len(e)) * 100 * 2.0e-3                       # ps
-    finite = np.isfinite(e).all()
-    slope = float(np.polyfit(t, e, 1)[0]) if finite else float("nan")
+    slope1, _, stop1 = _nve(p, sysm)
+    slope_l, ke_l, stop_l = _nve(_params(liq, acc, order, bins, exact), liq)
     return {"accumulation": acc, "eval": "direct" if order == 0 else f"order{order}",
-            "bins": None if order == 0 else bins, "err_max_over_rms": emax, "err_median": emed,
+            "bins": None if order == 0 else bins, "exact_differences": exact,
+            "err_max_over_rms": emax, "err_median": emed,
             "bit_reproducible": bool(np.array_equal(F1.view(np.uint32), F2.view(np.uint32))),
-            "nve_drift_kcal_per_mol_per_ps": slope, "e_total_first": float(e[0]), "e_total_last": float(e[-1]),
-            "steps": 10000, "dt_fs": 2.0}
+            "lj1728_nve_drift_kcal_per_mol_per_ps": slope1, "lj1728_range_error_at_step": stop1,
+            "liquid_nve_drift_kcal_per_mol_per_ps": slope_l, "liquid_mean_kinetic_kcal_per_mol": ke_l,
+            "liquid_range_error_at_step": stop_l, "steps": STEPS, "dt_fs": DT}
 
 
 def test_precision_sweep():
     sysm = systems.lj1728()
-    rows = [_variant(sysm, acc, order, bins) for acc in ACC for (_, order, bins) in EVALS]
+    liq = liquid_argon()
+    rows = [_variant(sysm, liq, acc, order, bins) for acc in ACC for (_, order, bins) in EVALS]
+    rows += [_variant(sysm, liq, acc, 2, 512, exact=True) for acc in ACC]
     out = os.environ.get("MDRL_REPORT_DIR")
     if out:
         with open(os.path.join(out, "precision_sweep.json"), "w") as fh:
             json.dump(rows, fh, indent=1)
-    by = {(r["accumulation"], r["eval"], r["bins"]): r for r in rows}
+    by = {(r["accumulation"], r["eval"], r["bins"], r["exact_differences"]): r for r in rows}
     for r in rows:
-        if r["accumulation"] == "fixed64":
-            assert r["bit_reproducible"], r                    # integer sums: order-independent
+        if r["accumulation"] != "fp32_atomic":
+            assert r["bit_reproducible"], r                    # fixed-order sums: order-independent
         assert r["err_median"] < 1e-2, r
+        assert r["liquid_range_error_at_step"] is None, r      # the liquid never leaves the range
+        assert np.isfinite(r["liquid_nve_drift_kcal_per_mol_per_ps"]), r
+        if r["bins"] is None or r["bins"] >= 256:
+            # the liquid conserves energy: drift over 20 ps below 5 % of its kinetic energy
+            assert abs(r["liquid_nve_drift_kcal_per_mol_per_ps"]) * 20.0 < 5e-2 * r["liquid_mean_kinetic_kcal_per_mol"], r
     # table error falls with the bin count (1st order)
-    assert by[("fixed64", "order1", 1024)]["err_median"] < by[("fixed64", "order1", 64)]["err_median"]
-    assert by[("fixed64", "order1", 1024)]["err_median"] <= 1e-5
+    assert by[("fixed64", "order1", 1024, False)]["err_median"] < by[("fixed64", "order1", 64, False)]["err_median"]
+    assert by[("fixed64", "order1", 1024, False)]["err_median"] <= 1e-5
+    # the exact-difference rule with bin-local order-2 tables meets 1e-5 in the primary norm
+    for acc in ACC:
+        assert by[(acc, "order2", 512, True)]["err_max_over_rms"] <= 1e-5

@@ -33,11 +33,13 @@ def sysm():
 
 @pytest.mark.parametrize("tile", [(4, 3, 0), (4, 12, 1), (8, 6, 1), (8, 1, 0), (4, 32, 1), (4, 6, 1)])
 @pytest.mark.parametrize("grid", ["3 cells", "4 cells"])
-def test_tile_parity_and_reproducibility(sysm, tile, grid):
+@pytest.mark.parametrize("exact", [False, True])
+def test_tile_parity_and_reproducibility(sysm, tile, grid, exact):
     if grid.startswith("4"):
         sysm = systems.small_ljc(6400, 50.0, 12.0, seed=22)
         assert sysm.ncell == (4, 4, 4)
-    p = sysm.params(table_bins=512, flags=m.FLAG_ENERGY)
+    p = sysm.params(table_bins=512, table_order=2 if exact else 1,
+                    flags=m.FLAG_ENERGY | (m.FLAG_EXACT_DIFF if exact else 0))
     x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
     with m.Context(p) as ctx:
         ctx.set_tile(*tile)

@@ -97,6 +97,35 @@ def test_fitters_agree():
         a = oracle.fit_tables(order, 8, bins, -2)
         b = m.fit_tables(order, 8, bins, -2)
         assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) < 1e-5
+    for order, bins in ((2, 256), (3, 128), (2, 1024)):           # the bin-local form
+        a = oracle.fit_tables(order, 8, bins, -2, local=True)
+        b = m.fit_tables(order, 8, bins, -2, local=True)
+        assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)) < 1e-5
+
+
+def test_bin_local_form_evaluates_like_the_monomial_form():
+    """The same least-squares polynomial in either form: evaluated in FP64 at points across each
+    bin, the bin-local and the monomial coefficients agree to the monomial form's FP32 coefficient
+    rounding (which cancellation amplifies) -- and the local form is the closer one to the
+    function itself."""
+    order, nseg, bins, m0 = 2, 8, 256, -2
+    mono = m.fit_tables(order, nseg, bins, m0).astype(np.float64)
+    loc = m.fit_tables(order, nseg, bins, m0, local=True).astype(np.float64)
+    idx = np.arange(nseg * bins)
+    seg, b = np.divmod(idx, bins)
+    x0 = np.ldexp(1.0 + b / bins, m0 + seg)
+    w = np.ldexp(1.0, m0 + seg) / bins
+    expo = np.array([-7.0, -4.0, -1.5, -6.0, -3.0, -0.5])
+    for frac in (0.1, 0.5, 0.9):
+        x = x0 + frac * w
+        u = x - x0
+        for f in range(6):
+            pm = mono[f, 0] + x * (mono[f, 1] + x * mono[f, 2])
+            pl = loc[f, 0] + u * (loc[f, 1] + u * loc[f, 2])
+            exact = x ** expo[f]
+            em, el = np.abs(pm - exact) / exact, np.abs(pl - exact) / exact
+            assert el.max() < 2e-7, (f, frac, el.max())
+            assert el.max() <= em.max(), (f, frac)
 
 
 def _ref_lines():

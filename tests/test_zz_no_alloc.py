@@ -34,16 +34,42 @@ def _static_forces(p, s):
     return torch.stack([fx, fy, fz], 1).cpu().numpy(), pairs
 
 
+def _compare(s, p):
+    with m.Context(p) as ctx:
+        F_ref, st, _ = ctx.force(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.q, s.type)
+    F, pairs = _static_forces(p, s)
+    assert pairs == st["pairs"]
+    assert np.isfinite(F).all()
+    assert (np.abs(F - F_ref) <= SUM_TOL * np.abs(F_ref) + FIX_ABS).all()
+
+
 def test_static_entry_point_matches_context_entry_point_twice():
-    systems_in_order = [systems.small_ljc(6000, 49.6, 12.0, seed=41), systems.small_ljc(3500, 49.6, 12.0, seed=42)]
-    for s in systems_in_order:
-        p = s.params(table_bins=1024)
-        with m.Context(p) as ctx:
-            F_ref, st, _ = ctx.force(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.q, s.type)
-        F, pairs = _static_forces(p, s)
-        assert pairs == st["pairs"]
-        assert np.isfinite(F).all()
-        assert (np.abs(F - F_ref) <= SUM_TOL * np.abs(F_ref) + FIX_ABS).all()
+    """Two different systems in a row with the same parameters: the second call reuses the tables
+    the first copied in and must clear the first call's leftovers."""
+    for s in [systems.small_ljc(6000, 49.6, 12.0, seed=41), systems.small_ljc(3500, 49.6, 12.0, seed=42)]:
+        _compare(s, s.params(table_bins=1024))
+
+
+def test_static_entry_point_refits_tables_when_parameters_change():
+    """Calls whose table order, bins, evaluation mode or force field differ from the previous
+    call's: each must refit and copy its own tables into the array (and the last call switches
+    back to the first call's parameters)."""
+    s = systems.small_ljc(5000, 49.6, 12.0, seed=44)
+    base = s.params(table_bins=1024)
+    other = s.params(table_bins=256, table_order=2)
+    other.sigma[1], other.epsilon[1] = 3.0, 0.1
+    direct = s.params(eval=m.EVAL_DIRECT)
+    for p in (base, other, direct, base):
+        _compare(s, p)
+
+
+def test_static_entry_point_rejects_another_device():
+    s = systems.small_ljc(64, 49.6, 12.0, seed=45)
+    p = s.params()
+    p.device = torch.cuda.current_device() + 1
+    with pytest.raises(m.MdrlError) as e:
+        m.force_eval_static(p, 10, 1, 1, 1, None, None, 1, 1, 1, None)
+    assert e.value.status == 1 and "current device" in str(e.value)
 
 
 def test_static_entry_point_rejects_sizes_beyond_its_limit():
