@@ -4,8 +4,12 @@
 A step is one velocity-Verlet MD step of the whole system on the GPU: kick + drift + rebin
 (count, scan, scatter, in-cell sort, gather), the half-shell force kernel, kick.  Default
 workload: the 92,224-atom LJ+Coulomb system (108.86 x 108.86 x 77.76 A, rc 12 A, 9x9x6 cells,
-4 types, +-0.42 e) with first-order 512-bin tables and int64 fixed-point accumulation ("tuned"),
-next to the FP32-atomic accumulation ("plain") at the same tables.
+4 types, +-0.42 e).  "tuned" = int64 fixed-point accumulation, autotuned tile, the exact-difference
+rule and bin-local order-2 512-bin tables (within 1e-5 of the FP64 oracle in max |dF| / rms |F|);
+"plain" = FP32-atomic accumulation and the default tile with the same datapath and tables;
+"reference_datapath" = the reference's difference rule and order-1 tables (pair list bit-equal to
+the reference's).  The same run also measures the 1,048,576-atom system and the 512-replica batch
+(sub-objects "ljc1m" and "batch512"), smooth PME and the bonded terms.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference] [--workload ...]
 
@@ -17,9 +21,10 @@ cell-list port) on rank 0 with every host thread.
 from __future__ import annotations
 
 import argparse
-import dataclasses
+import concurrent.futures as cf
 import ctypes as C
 import json
+import multiprocessing as mp
 import os
 import subprocess
 import sys
@@ -33,11 +38,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 FLOPS_PER_PAIR = 28            # algorithmic flops per in-cutoff pair, force only
+BYTES_PER_PARTICLE = 16 + 4 + 24   # pos+q and type read, int64 x3 force atomics, per force launch
 L2_FLUSH_BYTES = 256 << 20     # > 129 MB L2
 METRIC = "pair-evals/s & ns/day, 92k-atom RL LJ+Coulomb, tuned vs plain @1e-5 force err"
+CAPTURES = ROOT / "profiles" / "ncu_captures.json"   # per-capture ncu figures (workload, tile, datapath)
 
 
-def make_system(name: str, seed_offset: int):
+def make_system(name: str, seed_offset: int = 0):
     from sc2019_md_gb300 import systems
     if name == "ljc92k":
         return systems.ljc92k(seed_offset=seed_offset)
@@ -45,15 +52,27 @@ def make_system(name: str, seed_offset: int):
         return systems.lj1728(seed_offset=seed_offset)
     if name == "ljc1m":
         return systems.ljc1m(seed_offset=seed_offset)
+    if name == "batch512":
+        return systems.batch512()
     raise SystemExit(f"unknown workload {name}")
 
 
-def workload_desc(sysm, order, bins) -> str:
+def workload_desc(sysm) -> str:
     nc = "x".join(str(c) for c in sysm.ncell)
     box = "x".join(f"{b:g}" for b in sysm.box)
     kind = "LJ+Coulomb" if sysm.coulomb_k else "LJ"
     return (f"{sysm.name}: {sysm.n} atoms, {box} A periodic, rc {sysm.cutoff:g} A, {nc} cells, "
-            f"{len(sysm.sigma)} types, {kind}, order-{order} {bins}-bin tables, velocity Verlet 2 fs")
+            f"{len(sysm.sigma)} types, {kind}, velocity Verlet 2 fs")
+
+
+def method_desc(order: int, bins: int, exact: bool) -> str:
+    form = "bin-local" if order >= 2 else "monomial"
+    return (f"order-{order} {bins}-bin {form} tables, "
+            + ("exact minimum-image differences" if exact else "reference difference rule fl(fl(xi-xj)+-L)"))
+
+
+def tile_str(t) -> str:
+    return f"{t[0]}x{t[1]}x{t[2]} (warps per CTA x j-steps per piece x pruning)"
 
 
 class Clocks:
@@ -61,7 +80,7 @@ class Clocks:
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, index: int):
         self.index = index
@@ -78,6 +97,7 @@ class Clocks:
             self.reader.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -93,24 +113,32 @@ class Clocks:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.reader.join(timeout=2)
-        sm, mx, reasons = [], [], set()
+        sm, mx, busy, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for l in self.lines:
             f = [v.strip() for v in l.split(",")]
-            if len(f) < 7:
+            if len(f) < 8:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
+                s, mxv = float(f[0]), float(f[1])
             except ValueError:
                 continue
+            try:
+                u = float(f[7])
+            except ValueError:
+                u = 1.0
+            sm.append(s)
+            mx.append(mxv)
+            busy.append(u)
             for k, nm in enumerate(names):
                 if f[3 + k].lower() == "active":
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        loaded = [s for s, u in zip(sm, busy) if u > 0] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm), "samples_under_load": len([u for u in busy if u > 0]),
+                "window": "from the autotuner's timings through the timed steps"}
 
 
 def dist_setup(args):
@@ -147,32 +175,61 @@ def measured_peaks() -> dict:
     return {}
 
 
-def committed_metric(workload: str, key: str):
-    """A figure of the committed ncu summary profiles/k_force_<workload>.md ("<key>: <value> ...")."""
-    f = ROOT / "profiles" / f"k_force_{workload}.md"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        if line.startswith(key + ":"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+def ncu_capture(workload: str, tile, order: int, bins: int, exact: bool, min_log2: int) -> dict:
+    """The committed ncu figures for this kernel configuration, or a record saying none matches.
+    Each capture names the tile, tables and datapath it was taken with; figures of another
+    configuration are not reported for this one."""
+    want = {"workload": workload, "tile": list(tile), "order": order, "bins": bins, "exact": bool(exact),
+            "table_min_log2": min_log2}
+    try:
+        caps = json.loads(CAPTURES.read_text())
+    except (OSError, json.JSONDecodeError):
+        caps = []
+    for c in caps:
+        if all(c.get(k) == v for k, v in want.items()):
+            return {"matched": True, "source": f"profiles/{CAPTURES.name}", **c}
+    near = [c for c in caps if c.get("workload") == workload]
+    return {"matched": False, "source": f"profiles/{CAPTURES.name}", "wanted": want,
+            "captured": [{k: c.get(k) for k in want if k != "workload"} for c in near]}
 
 
-def committed_traffic(workload: str):
-    """Per-launch DRAM bytes of the force kernel from the committed ncu summary, or None."""
-    f = ROOT / "profiles" / f"k_force_{workload}.md"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+def fp32_peak_tflops(props, mhz: float) -> float:
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def _generate(name: str):
+    """Worker of the spawned generation pool (no CUDA in this process)."""
+    return make_system(name)
+
+
+class Flush:
+    def __init__(self, device):
+        import torch
+        self.buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    def __call__(self):
+        import torch
+        self.buf.zero_()
+        torch.cuda.synchronize()
+
+
+def md_leg(m, obj, steps: int, warmup: int, flush, nkernel: int = 12):
+    """Warm-up steps, then `steps` timed steps one graph launch each (L2 flushed before each);
+    then the force kernel alone nkernel times.  obj is a Context or Batch with state set."""
+    obj.step(warmup)
+    dev_ms, pairs, pstep = 0.0, 0, []
+    for _ in range(steps):
+        flush()
+        st = obj.step(1)
+        dev_ms += st["device_ms"]
+        pairs += st["pairs_total"]
+        pstep.append(st["pairs"])
+    fms = []
+    for _ in range(nkernel):
+        flush()
+        fms.append(obj.time_force())
+    return {"dev_ms": dev_ms, "pairs": pairs, "pairs_per_step": float(np.mean(pstep)) if pstep else 0.0,
+            "force_ms": float(np.median(fms)), "steps": steps}
 
 
 def force_eval_pinned(m, ctx, bufs, n):
@@ -189,305 +246,44 @@ def force_eval_pinned(m, ctx, bufs, n):
     return st
 
 
-def run_ours(args, rank, world, local, dist):
+def e2e_leg(m, params, sysm, tile, warmup: int, calls: int, flush):
+    """mdrl_force_eval end to end on pinned host buffers, host-timed per call."""
     import torch
-
-    import sc2019_md_gb300 as m
-    from sc2019_md_gb300 import systems
-
-    torch.cuda.set_device(local)
-    sysm = make_system(args.workload, rank)
-    params = sysm.params(table_bins=args.bins, table_order=args.order, device=local)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
-
-    def timed_steps(ctx, k):
-        dev_ms, pairs, fms, pstep = 0.0, 0, [], []
-        for _ in range(k):
-            flush.zero_()
-            torch.cuda.synchronize()
-            st = ctx.step(1)
-            dev_ms += st["device_ms"]
-            pairs += st["pairs_total"]
-            fms.append(st["force_ms"])
-            pstep.append(st["pairs"])
-        return dev_ms, pairs, fms, pstep
-
-    def barrier():
-        torch.cuda.synchronize()
-        if dist is not None:
-            dist.barrier()
-
-    # ---- tuned: int64 fixed point, autotuned tile -------------------------------------------
-    ctx = m.Context(params)
-    ctx.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
-    if args.tile:
-        ctx.set_tile(*args.tile)
-        tune = {"tile": ctx.tile(), "ms": None, "default_ms": None}
-    else:
-        tune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile(), "ms": None, "default_ms": None}
-    timed_steps(ctx, args.warmup)
-    barrier()
-    clocks = Clocks(local)
-    clocks.start()
-    t0 = time.perf_counter()
-    dev_ms, pairs, fms, pstep = timed_steps(ctx, args.steps)
-    barrier()
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    fms = []
-    for _ in range(max(3, min(args.steps, 20))):      # the force kernel alone, L2 flushed
-        flush.zero_()
-        torch.cuda.synchronize()
-        fms.append(ctx.time_force())
-    ctx.close()
-
-    # ---- the same step with smooth-PME long-range electrostatics (charged systems) -----------
-    pme_out = None
-    if not args.no_pme and sysm.q is not None:
-        ctxl = m.Context(params)
-        pme_p = ctxl.set_pme(order=args.pme_order)
-        ctxl.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
-        if not args.no_tune:
-            ctxl.autotune(retime=True)
-        timed_steps(ctxl, args.warmup)
-        kl = max(3, min(args.steps, 50))
-        ldev_ms, lpairs, _, _ = timed_steps(ctxl, kl)
-        ctxl.close()
-        pme_out = {"value": lpairs / (ldev_ms * 1e-3), "unit": "pair-evals/s", "ms_per_step": ldev_ms / kl,
-                   "ns_per_day": (1000.0 / (ldev_ms / kl)) * params.dt_fs * 0.0864, "steps": kl,
-                   "beta": pme_p["beta"], "grid": list(pme_p["grid"]), "order": pme_p["order"],
-                   "note": "same step + PME reciprocal part (spread, 2 FFTs, gather); real space in the pair tables"}
-
-    # ---- bonded terms: their kernels alone, on a chain topology of the same size ------------
-    bonded_out = None
-    if not args.no_bonded:
-        nch = sysm.n // 30
-        Lc = float((nch * 30 / 0.1) ** (1.0 / 3.0))
-        csys, T = systems.chains(nch, 30, Lc, seed=20191117 + 6, cutoff=12.0, dmin=0.0)
-        ctxb = m.Context(csys.params(table_bins=args.bins, table_order=args.order, device=local))
-        ctxb.set_bonded(**T)
-        ctxb.set_state(csys.pos[:, 0], csys.pos[:, 1], csys.pos[:, 2], csys.vel, None, csys.type)
-        bms = []
-        for _ in range(max(3, min(args.steps, 20))):
-            flush.zero_()
-            torch.cuda.synchronize()
-            bms.append(ctxb.time_bonded())
-        ctxb.close()
-        nterms = sum(len(v[0]) for v in T.values())
-        bmed = float(np.median(bms))
-        bonded_out = {"terms": nterms, "bonds": len(T["bonds"][0]), "angles": len(T["angles"][0]),
-                      "dihedrals": len(T["dihedrals"][0]), "ms": bmed, "terms_per_s": nterms / (bmed * 1e-3),
-                      "workload": f"{csys.n} atoms as {nch} chains of 30 in a {Lc:.1f} A cube (density 0.1), "
-                                  f"FP32 terms into the int64 accumulators; kernels alone (inverse map + terms), "
-                                  f"L2 flushed"}
-
-    # ---- plain: FP32 atomics, same tables --------------------------------------------------
-    kp = max(3, min(args.steps, 50))
-    pp = sysm.params(table_bins=args.bins, table_order=args.order, device=local, accum=m.ACC_FP32_ATOMIC)
-    ctxp = m.Context(pp)
-    ctxp.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
-    timed_steps(ctxp, args.warmup)
-    barrier()
-    pdev_ms, ppairs, pfms, _ = timed_steps(ctxp, kp)
-    barrier()
-    pfms = []
-    for _ in range(5):
-        flush.zero_()
-        torch.cuda.synchronize()
-        pfms.append(ctxp.time_force())
-    ctxp.close()
-
-    # ---- e2e: mdrl_force_eval on pinned host buffers ---------------------------------------
     n = sysm.n
     pin = lambda dt: torch.empty(n, dtype=dt, pin_memory=True).numpy()
     bufs = {k: pin(torch.float32) for k in ("x", "y", "z", "q", "fx", "fy", "fz")}
     bufs["t"] = pin(torch.int32)
-    for k, v in (("x", sysm.pos[:, 0]), ("y", sysm.pos[:, 1]), ("z", sysm.pos[:, 2]), ("q", sysm.q), ("t", sysm.type)):
+    for k, v in (("x", sysm.pos[:, 0]), ("y", sysm.pos[:, 1]), ("z", sysm.pos[:, 2]), ("q", sysm.q),
+                 ("t", sysm.type)):
         bufs[k][:] = v
-    ctxe = m.Context(params)
-    ctxe.set_tile(*tune["tile"])                       # the tile the tuned arm runs
-    for _ in range(args.warmup):
-        force_eval_pinned(m, ctxe, bufs, n)
-    ke = max(3, min(args.steps, 30))
-    e2e_s, e2e_pairs, e2e_dev = 0.0, 0, 0.0
-    for _ in range(ke):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        st = force_eval_pinned(m, ctxe, bufs, n)
-        e2e_s += time.perf_counter() - t1
-        e2e_pairs += st.pairs
-        e2e_dev += st.device_ms
-    ctxe.close()
-
-    # ---- reduce over ranks -----------------------------------------------------------------
-    mx, sm = combine_ranks(dist, f"cuda:{local}", maxes=[dev_ms, e2e_s, pdev_ms],
-                           sums=[pairs, e2e_pairs, ppairs])
-    if rank != 0:
-        return None
-    dev_ms_max = mx[0]
-    tot, psum, emax = [mx[0]], sm, [mx[1], mx[2]]
-    value = float(psum[0]) / (dev_ms_max * 1e-3)
-    ms_per_step = dev_ms_max / args.steps
-    ns_day = (1000.0 / ms_per_step) * params.dt_fs * 0.0864
-    force_s = float(np.mean(fms)) * 1e-3
-    pairs_launch = float(np.mean(pstep))
-    achieved_tf = pairs_launch * FLOPS_PER_PAIR / force_s / 1e12
-    props = torch.cuda.get_device_properties(local)
-    max_mhz = clk.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
-    fp32_peak = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
-    hbm_peak = measured_peaks().get("hbm_gbs")
-    alg_bytes = sysm.n * (16 + 4 + 24)   # pos+q, type read; int64 x3 force atomics
-    out = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "pair-evals/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": ms_per_step,
-        "ns_per_day": ns_day,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic (seeded; shapes of the reference's ApoA1 dataset)",
-        "config": {"workload": workload_desc(sysm, params.table_order, params.table_bins),
-                   "accumulation": "int64 fixed point 2^-24 (tuned)", "parallelism": f"replicas x{world}",
-                   "tile": {"warps_per_cta": tune["tile"][0], "steps_per_piece": tune["tile"][1],
-                            "prune_steps": tune["tile"][2],
-                            "autotuned": not (args.no_tune or args.tile), "force_ms_tuned": tune["ms"],
-                            "force_ms_default_tile": tune["default_ms"]},
-                   "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
-                   "pairs_per_step": pairs_launch},
-        "plain": {"value": float(psum[2]) / (float(emax[1]) * 1e-3), "unit": "pair-evals/s",
-                  "ms_per_step": float(emax[1]) / kp, "accumulation": "FP32 atomics, default tile (4 warps, 6 steps, no pruning)",
-                  "steps": kp,
-                  "force_ms": float(np.mean(pfms))},
-        "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak, "traffic": committed_traffic(args.workload),
-                     "kernel": "k_force (half-shell pair force)", "force_ms": force_s * 1e3,
-                     "flops_per_pair": FLOPS_PER_PAIR,
-                     "fma_pipe_active_pct_ncu": committed_metric(args.workload, "fma_pipe_active_pct"),
-                     "peak_source": f"computed: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop x "
-                                    f"{max_mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"},
-        "roofline_hbm": {"achieved": alg_bytes / force_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": (alg_bytes / force_s / 1e9 / hbm_peak) if hbm_peak else None,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                         "algorithmic_bytes_per_launch": alg_bytes},
-        "e2e": {"value": float(psum[1]) / float(emax[0]), "unit": "pair-evals/s",
-                "h2d_bytes_per_step": n * 20, "d2h_bytes_per_step": n * 12,
-                "call": "mdrl_force_eval (pinned host x,y,z,q,type in; fx,fy,fz out)", "calls": ke,
-                "ms_per_call": e2e_s / ke * 1e3, "device_ms_per_call": e2e_dev / ke,
-                "host_link": "pinned buffers read and written in place by the binning and unsort kernels"},
-        "with_pme": pme_out,
-        "bonded": bonded_out,
-        "gpu_launches": 8 * args.steps,
-        "clocks": clk,
-        "wall_s": wall,
-    }
-    if world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"], out["force_error"], out["cpu_baseline_allpairs"] = cpu_baseline(sysm, params, args)
-    return out
+    with m.Context(params) as ctx:
+        ctx.set_tile(*tile)
+        for _ in range(warmup):
+            force_eval_pinned(m, ctx, bufs, n)
+        secs, pairs, dev = 0.0, 0, 0.0
+        for _ in range(calls):
+            flush()
+            t1 = time.perf_counter()
+            st = force_eval_pinned(m, ctx, bufs, n)
+            secs += time.perf_counter() - t1
+            pairs += st.pairs
+            dev += st.device_ms
+    return {"secs": secs, "pairs": pairs, "calls": calls, "dev_ms": dev, "n": n}
 
 
-def run_batch(args, rank, world, local, dist):
-    """512 independent replicas (N log-uniform 500-20,000, rc 10 A): all of them per step in one
-    graph launch, against the same replicas stepped one at a time (each its own graph)."""
-    import torch
-
-    import sc2019_md_gb300 as m
-    from sc2019_md_gb300 import systems
-
-    torch.cuda.set_device(local)
-    t0 = time.perf_counter()
-    reps = systems.batch512(args.replicas)
-    gen_s = time.perf_counter() - t0
-    pos, vel, q, t, spec = systems.concat(reps)
-    params = reps[0].params(table_bins=args.bins, table_order=args.order, device=local)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
-
-    b = m.Batch(params, spec)
-    lay = b.layout()
-    b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
-    tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6, 0), "ms": None, "default_ms": None}
-    b.step(args.warmup)
-    torch.cuda.synchronize()
-    clocks = Clocks(local)
-    clocks.start()
-    dev_ms, pairs, pstep = 0.0, 0, []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        st = b.step(1)
-        dev_ms += st["device_ms"]
-        pairs += st["pairs_total"]
-        pstep.append(st["pairs"])
-    clk = clocks.stop()
-    fms = []
-    for _ in range(5):
-        flush.zero_()
-        torch.cuda.synchronize()
-        fms.append(b.time_force())
-    b.close()
-
-    # the same replicas one by one: a batch of one replica each, stepped in turn
-    k1 = max(3, min(args.steps, 20))
-    one_ms, one_pairs = 0.0, 0
-    for r, s in enumerate(reps):
-        with m.Batch(params, [spec[r]]) as b1:
-            b1.set_state(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.vel, s.q, s.type)
-            b1.step(1)
-            st = b1.step(k1)
-            one_ms += st["device_ms"]
-            one_pairs += st["pairs_total"]
-    value = pairs / (dev_ms * 1e-3)
-    ms_step = dev_ms / args.steps
-    force_s = float(np.mean(fms)) * 1e-3
-    props = torch.cuda.get_device_properties(local)
-    max_mhz = clk.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
-    fp32_peak = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
-    achieved_tf = float(np.mean(pstep)) * FLOPS_PER_PAIR / force_s / 1e12
-    npath = np.bincount(lay["path"], minlength=3)
-    return {
-        "metric": "pair-evals/s, batched replicas (one launch per kernel per step) vs one by one",
-        "value": value, "unit": "pair-evals/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded replicas)",
-        "config": {"workload": f"batch{len(reps)}: {len(reps)} replicas, {int(b.n)} atoms, N log-uniform "
-                               f"500-20000 at 0.1 /A^3, rc 10 A, argon-like +-0.42 e, order-{args.order} "
-                               f"{args.bins}-bin tables, int64 fixed point, velocity Verlet 2 fs",
-                   "paths": {"half_shell": int(npath[0]), "min_image": int(npath[1]), "all_images": int(npath[2])},
-                   "work_items": int(lay["total_items"]), "pairs_per_step": float(np.mean(pstep)),
-                   "tile": {"steps_per_piece": tune["tile"][1], "prune_steps": tune["tile"][2],
-                            "autotuned": not args.no_tune,
-                            "force_ms_tuned": tune["ms"], "force_ms_default_tile": tune["default_ms"]},
-                   "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
-                   "generation_s": gen_s},
-        "one_by_one": {"value": one_pairs / (one_ms * 1e-3), "unit": "pair-evals/s", "steps": k1,
-                       "ms_per_step": one_ms / k1,
-                       "how": "a batch of one replica each (default tile), stepped in turn, each its own graph"},
-        "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak, "traffic": committed_traffic("batch512"),
-                     "kernel": "k_force (batched work list)",
-                     "force_ms": force_s * 1e3, "flops_per_pair": FLOPS_PER_PAIR,
-                     "fma_pipe_active_pct_ncu": committed_metric("batch512", "fma_pipe_active_pct")},
-        "gpu_launches": 9 * args.steps,
-        "clocks": clk,
-    }
-
-
-def oracle_system(sysm, order, bins, arith=0):
-    import oracle
-    T = len(sysm.sigma)
-    pc64 = oracle.lb_coefficients(sysm.sigma, sysm.epsilon)
-    m0 = -2
-    rc2 = np.float32(np.float32(sysm.cutoff) * np.float32(sysm.cutoff))
-    nseg = int(np.floor(np.log2(rc2))) - m0 + 1
-    tab = oracle.fit_tables(order, nseg, bins, m0)
-    return oracle.System(sysm.pos, sysm.box, sysm.ncell, sysm.cutoff, pc64.astype(np.float32), q=sysm.q,
-                         type=sysm.type, ke=sysm.coulomb_k, tab=tab, order=order, nseg=nseg, bins=bins,
-                         min_log2=m0, arith=arith, pcoef64=pc64, ke64=sysm.coulomb_k)
+def roofline(pairs_per_launch: float, force_ms: float, n: int, props, mhz: float, capture: dict) -> dict:
+    achieved = pairs_per_launch * FLOPS_PER_PAIR / (force_ms * 1e-3) / 1e12
+    peak = fp32_peak_tflops(props, mhz)
+    alg_bytes = n * BYTES_PER_PARTICLE
+    hbm = measured_peaks().get("hbm_gbs")
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": capture.get("dram_bytes_per_launch") if capture.get("matched") else None,
+            "kernel": "k_force (half-shell pair force)", "force_ms": force_ms, "flops_per_pair": FLOPS_PER_PAIR,
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "hbm_achieved_gbs": alg_bytes / (force_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm,
+            "peak_source": f"computed: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz "
+                           f"(MEASURED_PEAKS.json has no FP32 figure); hbm_peak_gbs of measured",
+            "ncu_summary": capture}
 
 
 def _force_error(F, Fref, vs):
@@ -497,63 +293,358 @@ def _force_error(F, Fref, vs):
             "median_rel": float(np.median(d / np.maximum(nrm, 1e-30)))}
 
 
-def cpu_baseline(sysm, params, args):
-    """The oracle's multi-threaded cell-list port on the host cores (bounded sample), a bounded
-    sample of the C model's all-pairs restatement, and the force error of the GPU's first
-    evaluation (tuned and plain) against the FP64 direct oracle and the FP64 evaluation of the
-    same tables."""
-    import sc2019_md_gb300 as m
-    o = oracle_system(sysm, params.table_order, params.table_bins)
-    cores = os.cpu_count() or 1
-    o.force_cells_mt(cores)                                   # warm
+def oracle_system(sysm, order, bins, arith=0, exact=False):
+    import oracle
+    pc64 = oracle.lb_coefficients(sysm.sigma, sysm.epsilon)
+    m0 = sysm.table_min_log2
+    rc2 = np.float32(np.float32(sysm.cutoff) * np.float32(sysm.cutoff))
+    nseg = int(np.floor(np.log2(rc2))) - m0 + 1
+    tab = oracle.fit_tables(order, nseg, bins, m0, local=order >= 2)
+    return oracle.System(sysm.pos, sysm.box, sysm.ncell, sysm.cutoff, pc64.astype(np.float32), q=sysm.q,
+                         type=sysm.type, ke=sysm.coulomb_k, tab=tab, order=order, nseg=nseg, bins=bins,
+                         min_log2=m0, arith=arith, pcoef64=pc64, ke64=sysm.coulomb_k, local=order >= 2,
+                         exact=exact)
+
+
+def cpu_port_rate(o, cores: int, budget_s: float = 10.0):
+    """The oracle's OpenMP half-shell port: full force evaluations for about budget_s seconds."""
+    o.force_cells_mt(cores)
     t0 = time.perf_counter()
     pairs, calls = 0, 0
-    while calls < 3 or (time.perf_counter() - t0 < 10.0 and calls < 40):
+    while calls < 3 or (time.perf_counter() - t0 < budget_s and calls < 40):
         _, p = o.force_cells_mt(cores)
         pairs += p
         calls += 1
     el = time.perf_counter() - t0
-    base = {"value": pairs / el, "unit": "pair-evals/s", "cores": cores, "kind": "port",
-            "sample": f"{calls} full force evaluations of the same system (half-shell cell list, "
-                      f"FP32, OpenMP over home cells)", "seconds": el}
-    # the C model's all-pairs O(N^2) form: every ordered pair of the first n_ap particles tested,
-    # the test rate extrapolated to the full system's N^2 tests and set against the pairs one
-    # cell-list evaluation of the full system finds
-    n_ap = min(sysm.n, 24000)
-    prefix = dataclasses.replace(sysm, pos=sysm.pos[:n_ap], vel=sysm.vel[:n_ap], type=sysm.type[:n_ap],
-                                 q=None if sysm.q is None else sysm.q[:n_ap])
-    sub = oracle_system(prefix, params.table_order, params.table_bins)
-    t1 = time.perf_counter()
-    sub.force_allpairs_mt(cores)
-    el_ap = time.perf_counter() - t1
-    tests_per_s = n_ap * n_ap / el_ap
-    full_s = float(sysm.n) ** 2 / tests_per_s
-    base_ap = {"value": (pairs / calls) / full_s, "unit": "pair-evals/s", "cores": cores, "kind": "port",
-               "sample": f"all {n_ap}^2 ordered pair tests of the first {n_ap} particles (C-model all-pairs "
-                         f"form, FP32, OpenMP over i), extrapolated to {sysm.n}^2 tests",
-               "pair_tests_per_s": tests_per_s, "full_eval_s": full_s, "seconds": el_ap}
-    with m.Context(params) as ctx:
-        F, _, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
-    pp = sysm.params(table_bins=params.table_bins, table_order=params.table_order, device=params.device,
-                     accum=m.ACC_FP32_ATOMIC)
-    with m.Context(pp) as ctx:
-        Fp, _, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
-    F64, _ = o.force_direct64()
-    Ft, _ = o.force_tables64()
-    err = {"tuned": [_force_error(F, F64, "FP64 direct oracle, same pair set"),
-                     _force_error(F, Ft, "FP64 evaluation of the same tables")],
-           "plain": [_force_error(Fp, F64, "FP64 direct oracle, same pair set"),
-                     _force_error(Fp, Ft, "FP64 evaluation of the same tables")]}
-    return base, err, base_ap
+    return pairs / el, calls, el
+
+
+def accuracy(m, sysm, legs: dict) -> dict:
+    """Force error of each leg's first evaluation against the FP64 direct oracle (and the FP64
+    evaluation of the same tables), both stated norms."""
+    out, cache = {}, {}
+    for name, (params, order, bins, exact) in legs.items():
+        with m.Context(params) as ctx:
+            F, _, _ = ctx.force(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
+        key = (order, bins, exact)
+        if key not in cache:
+            o = oracle_system(sysm, order, bins, exact=exact)
+            cache[key] = (o.force_direct64()[0], o.force_tables64()[0])
+        F64, Ft = cache[key]
+        out[name] = [_force_error(F, F64, "FP64 direct oracle, same pair set"),
+                     _force_error(F, Ft, "FP64 evaluation of the same tables")]
+    return out
+
+
+def single_system(m, sysm, args, local, flush, clocks=None, barrier=lambda: None):
+    """Tuned (timed, autotuned), plain and reference-datapath legs of one system."""
+    base = dict(table_bins=args.bins, device=local)
+    exact = args.datapath == "exact"
+    fl = m.FLAG_EXACT_DIFF if exact else 0
+    p_tuned = sysm.params(table_order=args.order, flags=fl, **base)
+    p_plain = sysm.params(table_order=args.order, flags=fl, accum=m.ACC_FP32_ATOMIC, **base)
+    p_ref = sysm.params(table_order=1, **base)
+    st_args = (sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
+    out = {"params": {"tuned": p_tuned, "plain": p_plain, "reference_datapath": p_ref}}
+
+    with m.Context(p_tuned) as ctx:
+        ctx.set_state(*st_args)
+        if clocks is not None:
+            clocks.start()
+        if args.tile:
+            ctx.set_tile(*args.tile)
+            tune = {"tile": ctx.tile(), "ms": None, "default_ms": None}
+        elif args.no_tune:
+            tune = {"tile": ctx.tile(), "ms": None, "default_ms": None}
+        else:
+            tune = ctx.autotune(retime=True)
+        ctx.step(args.warmup)
+        barrier()
+        t0 = time.perf_counter()
+        leg = md_leg(m, ctx, args.steps, 0, flush, nkernel=max(3, min(args.steps, 20)))
+        barrier()
+        out["wall_s"] = time.perf_counter() - t0
+        out["clocks"] = clocks.stop() if clocks is not None else None
+    out["tuned"] = {**leg, "tile": tune["tile"], "tune": tune}
+
+    kp = max(3, min(args.steps, 50))
+    with m.Context(p_plain) as ctx:
+        ctx.set_state(*st_args)
+        out["plain"] = md_leg(m, ctx, kp, args.warmup, flush, nkernel=5)
+        out["plain"]["tile"] = ctx.tile()
+
+    with m.Context(p_ref) as ctx:
+        ctx.set_state(*st_args)
+        rtune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile()}
+        out["reference_datapath"] = md_leg(m, ctx, kp, args.warmup, flush, nkernel=5)
+        out["reference_datapath"]["tile"] = rtune["tile"]
+
+    out["e2e"] = e2e_leg(m, p_tuned, sysm, tune["tile"], args.warmup, max(3, min(args.steps, 30)), flush)
+    return out
+
+
+def sub_workload_single(m, sysm, args, local, flush, props):
+    """Tuned vs plain MD steps, kernel timing and e2e of a second single system (the 1M-atom one)."""
+    exact = args.datapath == "exact"
+    fl = m.FLAG_EXACT_DIFF if exact else 0
+    k = max(3, min(args.steps, 10))
+    p_t = sysm.params(table_order=args.order, table_bins=args.bins, device=local, flags=fl)
+    p_p = sysm.params(table_order=args.order, table_bins=args.bins, device=local, flags=fl,
+                      accum=m.ACC_FP32_ATOMIC)
+    st_args = (sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
+    with m.Context(p_t) as ctx:
+        ctx.set_state(*st_args)
+        tune = ctx.autotune(retime=True) if not args.no_tune else {"tile": ctx.tile(), "ms": None, "default_ms": None}
+        tuned = md_leg(m, ctx, k, args.warmup, flush, nkernel=5)
+    with m.Context(p_p) as ctx:
+        ctx.set_state(*st_args)
+        plain = md_leg(m, ctx, k, args.warmup, flush, nkernel=5)
+    e2e = e2e_leg(m, p_t, sysm, tune["tile"], 2, 3, flush)
+    mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    ms = tuned["dev_ms"] / k
+    return {
+        "workload": workload_desc(sysm) + "; " + method_desc(args.order, args.bins, exact),
+        "value": tuned["pairs"] / (tuned["dev_ms"] * 1e-3), "unit": "pair-evals/s", "steps": k,
+        "warmup": args.warmup, "ms_per_step": ms, "ns_per_day": (1000.0 / ms) * 2.0 * 0.0864,
+        "tile": tile_str(tune["tile"]), "force_ms_tuned_tile": tune.get("ms"),
+        "force_ms_default_tile": tune.get("default_ms"),
+        "plain": {"value": plain["pairs"] / (plain["dev_ms"] * 1e-3), "ms_per_step": plain["dev_ms"] / k,
+                  "force_ms": plain["force_ms"], "accumulation": "FP32 atomics, default tile, same datapath"},
+        "tuned_over_plain": (plain["dev_ms"] / tuned["dev_ms"]) if tuned["dev_ms"] else None,
+        "roofline": roofline(tuned["pairs_per_step"], tuned["force_ms"], sysm.n, props, mhz,
+                             ncu_capture(sysm.name, tune["tile"], args.order, args.bins, exact, sysm.table_min_log2)),
+        "e2e": {"value": e2e["pairs"] / e2e["secs"], "unit": "pair-evals/s", "h2d_bytes_per_step": sysm.n * 20,
+                "d2h_bytes_per_step": sysm.n * 12, "calls": e2e["calls"],
+                "ms_per_call": e2e["secs"] / e2e["calls"] * 1e3},
+        "pairs_per_step": tuned["pairs_per_step"],
+        "gpu_launches": 8 * k,
+    }
+
+
+def sub_workload_batch(m, reps, args, local, flush, props):
+    """The batched replicas: one graph launch per step for all of them, against the same replicas
+    stepped one at a time; kernel timing and e2e (host buffers through mdrl_batch_force_eval)."""
+    from sc2019_md_gb300 import systems
+    pos, vel, q, t, spec = systems.concat(reps)
+    params = reps[0].params(table_bins=args.bins, table_order=1, device=local)
+    k = max(3, min(args.steps, 10))
+    with m.Batch(params, spec) as b:
+        lay = b.layout()
+        b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
+        tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6, 0), "ms": None, "default_ms": None}
+        leg = md_leg(m, b, k, args.warmup, flush, nkernel=5)
+    with m.Batch(params, spec) as b:       # e2e: host arrays in and out (copies inside the call)
+        b.set_tile(*tune["tile"])
+        b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t)
+        e_secs, e_pairs = 0.0, 0
+        for _ in range(3):
+            flush()
+            t1 = time.perf_counter()
+            _, st, _ = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t)
+            e_secs += time.perf_counter() - t1
+            e_pairs += st["pairs"]
+    k1 = 3
+    one_ms, one_pairs = 0.0, 0
+    for r, s in enumerate(reps):
+        with m.Batch(params, [spec[r]]) as b1:
+            b1.set_state(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.vel, s.q, s.type)
+            b1.step(1)
+            st = b1.step(k1)
+            one_ms += st["device_ms"]
+            one_pairs += st["pairs_total"]
+    ntot = len(pos)
+    mhz = measured_peaks().get("sm_max_mhz") or 2070.0
+    npath = np.bincount(lay["path"], minlength=3)
+    value = leg["pairs"] / (leg["dev_ms"] * 1e-3)
+    one = one_pairs / (one_ms * 1e-3)
+    return {
+        "workload": (f"batch{len(reps)}: {len(reps)} replicas, {ntot} atoms, N log-uniform 500-20000 at 0.1 /A^3, "
+                     f"rc 10 A, argon-like +-0.42 e; order-1 {args.bins}-bin tables, reference difference rule, "
+                     f"int64 fixed point"),
+        "value": value, "unit": "pair-evals/s", "steps": k, "warmup": args.warmup,
+        "ms_per_step": leg["dev_ms"] / k, "tile": tile_str(tune["tile"]),
+        "paths": {"half_shell": int(npath[0]), "min_image": int(npath[1]), "all_images": int(npath[2])},
+        "work_items": int(lay["total_items"]),
+        "one_by_one": {"value": one, "unit": "pair-evals/s", "steps": k1, "ms_per_step": one_ms / k1,
+                       "how": "a batch of one replica each (default tile), stepped in turn, each its own graph"},
+        "batched_over_one_by_one": value / one if one else None,
+        "roofline": roofline(leg["pairs_per_step"], leg["force_ms"], ntot, props, mhz,
+                             ncu_capture("batch512", tune["tile"], 1, args.bins, False, reps[0].table_min_log2)),
+        "e2e": {"value": e_pairs / e_secs, "unit": "pair-evals/s", "h2d_bytes_per_step": ntot * 20,
+                "d2h_bytes_per_step": ntot * 12, "calls": 3, "ms_per_call": e_secs / 3 * 1e3,
+                "call": "mdrl_batch_force_eval (host x,y,z,q,type in; fx,fy,fz out)"},
+        "pairs_per_step": leg["pairs_per_step"],
+        "gpu_launches": 9 * k,
+    }
+
+
+def run_ours(args, rank, world, local, dist):
+    import torch
+
+    import sc2019_md_gb300 as m
+    from sc2019_md_gb300 import systems
+
+    # the larger workloads are generated on the host while the GPU measures the first one
+    extra = world == 1 and not args.no_extra and args.workload == "ljc92k"
+    pool = futs = None
+    if extra:
+        pool = cf.ProcessPoolExecutor(max_workers=2, mp_context=mp.get_context("spawn"))
+        futs = {name: pool.submit(_generate, name) for name in ("ljc1m", "batch512")}
+
+    torch.cuda.set_device(local)
+    sysm = make_system(args.workload, rank)
+    flush = Flush(f"cuda:{local}")
+    props = torch.cuda.get_device_properties(local)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    exact = args.datapath == "exact"
+    res = single_system(m, sysm, args, local, flush, Clocks(local), barrier)
+    tuned, plain, refd, e2e = res["tuned"], res["plain"], res["reference_datapath"], res["e2e"]
+    clk = res["clocks"]
+
+    # ---- the same step with smooth-PME long-range electrostatics (charged systems) -----------
+    pme_out = None
+    if not args.no_pme and sysm.q is not None:
+        with m.Context(res["params"]["tuned"]) as ctxl:
+            pme_p = ctxl.set_pme(order=args.pme_order)
+            ctxl.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
+            ctxl.set_tile(*tuned["tile"])
+            kl = max(3, min(args.steps, 50))
+            leg = md_leg(m, ctxl, kl, args.warmup, flush, nkernel=1)
+        pme_out = {"value": leg["pairs"] / (leg["dev_ms"] * 1e-3), "unit": "pair-evals/s",
+                   "ms_per_step": leg["dev_ms"] / kl, "ns_per_day": (1000.0 / (leg["dev_ms"] / kl)) * 2.0 * 0.0864,
+                   "steps": kl, "beta": pme_p["beta"], "grid": list(pme_p["grid"]), "order": pme_p["order"],
+                   "note": "same step + PME reciprocal part (spread, 2 FFTs, gather); real space in the pair tables"}
+
+    # ---- bonded terms: their kernels alone, on a chain topology of the same size ------------
+    bonded_out = None
+    if not args.no_bonded:
+        nch = sysm.n // 30
+        Lc = float((nch * 30 / 0.1) ** (1.0 / 3.0))
+        csys, T = systems.chains(nch, 30, Lc, seed=20191117 + 6, cutoff=12.0, dmin=0.0)
+        with m.Context(csys.params(table_bins=args.bins, device=local)) as ctxb:
+            ctxb.set_bonded(**T)
+            ctxb.set_state(csys.pos[:, 0], csys.pos[:, 1], csys.pos[:, 2], csys.vel, None, csys.type)
+            bms = []
+            for _ in range(max(3, min(args.steps, 20))):
+                flush()
+                bms.append(ctxb.time_bonded())
+        nterms = sum(len(v[0]) for v in T.values())
+        bmed = float(np.median(bms))
+        bonded_out = {"terms": nterms, "bonds": len(T["bonds"][0]), "angles": len(T["angles"][0]),
+                      "dihedrals": len(T["dihedrals"][0]), "ms": bmed, "terms_per_s": nterms / (bmed * 1e-3),
+                      "workload": f"{csys.n} atoms as {nch} chains of 30 in a {Lc:.1f} A cube (density 0.1), "
+                                  f"FP32 terms into the int64 accumulators; kernels alone (inverse map + terms), "
+                                  f"L2 flushed"}
+
+    # ---- reduce over ranks -----------------------------------------------------------------
+    mx, sm = combine_ranks(dist, f"cuda:{local}", maxes=[tuned["dev_ms"], e2e["secs"], plain["dev_ms"]],
+                           sums=[tuned["pairs"], e2e["pairs"], plain["pairs"]])
+    if rank != 0:
+        if pool:
+            pool.shutdown(cancel_futures=True)
+        return None
+    value = sm[0] / (mx[0] * 1e-3)
+    ms_per_step = mx[0] / args.steps
+    mhz = (clk or {}).get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
+    cap = ncu_capture(args.workload, tuned["tile"], args.order, args.bins, exact, sysm.table_min_log2)
+    kp = plain["steps"]
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "pair-evals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "ns_per_day": (1000.0 / ms_per_step) * 2.0 * 0.0864,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded; shapes of the reference's ApoA1 dataset)",
+        "config": {"workload": workload_desc(sysm), "method": method_desc(args.order, args.bins, exact),
+                   "accumulation": "int64 fixed point 2^-24 (tuned)", "parallelism": f"replicas x{world}",
+                   "tile": tile_str(tuned["tile"]), "autotuned": not (args.no_tune or args.tile),
+                   "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
+                   "pairs_per_step": tuned["pairs_per_step"]},
+        "plain": {"value": sm[2] / (mx[2] * 1e-3), "unit": "pair-evals/s", "ms_per_step": mx[2] / kp,
+                  "steps": kp, "force_ms": plain["force_ms"], "tile": tile_str(plain["tile"]),
+                  "accumulation": "FP32 atomics, default tile, same datapath and tables"},
+        "tuned_over_plain": mx[2] / kp / ms_per_step,
+        "reference_datapath": {"value": refd["pairs"] / (refd["dev_ms"] * 1e-3), "unit": "pair-evals/s",
+                               "ms_per_step": refd["dev_ms"] / refd["steps"], "force_ms": refd["force_ms"],
+                               "tile": tile_str(refd["tile"]), "method": method_desc(1, args.bins, False),
+                               "pairs_per_step": refd["pairs_per_step"],
+                               "note": "int64 fixed point, autotuned; pair list bit-equal to the reference's datapath"},
+        "roofline": roofline(tuned["pairs_per_step"], tuned["force_ms"], sysm.n, props, mhz, cap),
+        "e2e": {"value": sm[1] / mx[1], "unit": "pair-evals/s", "h2d_bytes_per_step": sysm.n * 20,
+                "d2h_bytes_per_step": sysm.n * 12,
+                "call": "mdrl_force_eval (pinned host x,y,z,q,type in; fx,fy,fz out)", "calls": e2e["calls"],
+                "ms_per_call": e2e["secs"] / e2e["calls"] * 1e3, "device_ms_per_call": e2e["dev_ms"] / e2e["calls"],
+                "host_link": "pinned buffers read and written in place by the binning and unsort kernels"},
+        "with_pme": pme_out,
+        "bonded": bonded_out,
+        "gpu_launches": 8 * args.steps,
+        "clocks": clk,
+        "wall_s": res["wall_s"],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        o = oracle_system(sysm, args.order, args.bins, exact=exact)
+        rate, calls, el = cpu_port_rate(o, cores)
+        out["cpu_baseline"] = {"value": rate, "unit": "pair-evals/s", "cores": cores, "kind": "port",
+                               "sample": f"{calls} full force evaluations of the same system and datapath "
+                                         f"(half-shell cell list, FP32, OpenMP over home cells)", "seconds": el}
+        out["force_error"] = accuracy(m, sysm, {
+            "tuned": (res["params"]["tuned"], args.order, args.bins, exact),
+            "plain": (res["params"]["plain"], args.order, args.bins, exact),
+            "reference_datapath": (res["params"]["reference_datapath"], 1, args.bins, False)})
+        out["force_error"]["norm"] = "max_i |dF_i| / rms_j |F_j| (primary); median_i |dF_i| / |F_i|"
+    if extra:
+        try:
+            out["ljc1m"] = sub_workload_single(m, futs["ljc1m"].result(), args, local, flush, props)
+            out["batch512"] = sub_workload_batch(m, futs["batch512"].result(), args, local, flush, props)
+        finally:
+            pool.shutdown()
+    return out
+
+
+def run_batch(args, rank, world, local, dist):
+    """The batched workload as the headline (--workload batch512)."""
+    import torch
+
+    import sc2019_md_gb300 as m
+
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    reps = make_system("batch512")
+    gen_s = time.perf_counter() - t0
+    flush = Flush(f"cuda:{local}")
+    props = torch.cuda.get_device_properties(local)
+    clocks = Clocks(local).start()
+    sub = sub_workload_batch(m, reps, args, local, flush, props)
+    clk = clocks.stop()
+    return {"metric": "pair-evals/s, batched replicas (one launch per kernel per step) vs one by one",
+            "n_gpus": world, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded replicas)", "clocks": clk, "generation_s": gen_s,
+            "config": {"workload": sub["workload"], "tile": sub["tile"],
+                       "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"},
+            **{k: v for k, v in sub.items() if k not in ("workload", "tile")}}
 
 
 def run_reference(args, rank, world):
-    """The CPU implementation of the path (oracle port), every host thread, rank 0 only."""
+    """The CPU implementation of the path (oracle port) on the same workload, datapath and tables,
+    every host thread, rank 0 only; each step is a bounded sample of the home cells."""
     if rank != 0:
         return None
-    import oracle
     sysm = make_system(args.workload, 0)
-    o = oracle_system(sysm, args.order, args.bins)
+    exact = args.datapath == "exact"
+    o = oracle_system(sysm, args.order, args.bins, exact=exact)
     cores = os.cpu_count() or 1
     ncells = int(np.prod(sysm.ncell))
     t0 = time.perf_counter()
@@ -577,8 +668,11 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)",
-        "config": {"workload": workload_desc(sysm, args.order, args.bins), "parallelism": "host threads"},
+        "data": "synthetic (seeded; shapes of the reference's ApoA1 dataset)",
+        "config": {"workload": workload_desc(sysm), "method": method_desc(args.order, args.bins, exact),
+                   "accumulation": "FP32 per-pair forces, FP64 sums (CPU port)",
+                   "parallelism": f"{cores} host threads", "tile": "none (CPU: OpenMP over home cells)",
+                   "autotuned": False, "l2": "host caches (CPU)", "pairs_per_step": pairs / args.steps},
         "cpu_baseline": {"value": value, "unit": "pair-evals/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -591,10 +685,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="ljc92k", choices=["ljc92k", "lj1728", "ljc1m", "batch512"])
+    ap.add_argument("--datapath", choices=["exact", "reference"], default="exact",
+                    help="difference rule of the tuned and plain arms (MDRL_FLAG_EXACT_DIFF or the reference's)")
     ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term kernel timing")
-    ap.add_argument("--replicas", type=int, default=512, help="batch512: number of replicas")
+    ap.add_argument("--no-extra", action="store_true", help="skip the 1M-atom and 512-replica sub-workloads")
     ap.add_argument("--bins", type=int, default=512)
-    ap.add_argument("--order", type=int, default=1)
+    ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile (no autotuning)")
     ap.add_argument("--tile", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,

@@ -264,6 +264,43 @@ mdrl_status mdrl_get_state(mdrl_ctx *ctx, float *x, float *y, float *z, float *v
  * context's stream; *ms receives the kernel's device time.  The state is not modified. */
 mdrl_status mdrl_time_force(mdrl_ctx *ctx, float *ms);
 
+/* ---- spatial decomposition of one system over ranks (slabs of cells along x) ---------------
+ * The partition the reference's strong-scaling model describes (MatlabScripts/
+ * SC19_MD_Strong_Scale_Performance.m:130-212): each rank owns a slab of whole cell layers along x;
+ * the half shell reaches one layer in +x only, so before the force pass a rank imports the first
+ * cell layer of the next rank's slab (positions, charges, types: the halo), evaluates every unit
+ * whose home cell lies in its slab -- halo particles receive their Newton-3 partial forces -- and
+ * returns the halo's int64 forces to their owner, which adds them (exact integer sums: the
+ * decomposed forces equal the single-domain ones bit for bit when each cell keeps its particles
+ * in the same relative order).  Host-side planning only; the exchange is the caller's (NCCL,
+ * MPI, ...).  No counterpart in the reference's code, which runs on one FPGA. */
+typedef struct {
+    int nranks, rank;
+    int x0, x1;        /* owned cell layers [x0, x1) along x */
+    int halo_x;        /* the imported layer: x1 modulo the layer count (the next rank's x0) */
+    int import_from;   /* rank owning halo_x: halo positions come from it, its forces go back */
+    int export_to;     /* rank that imports this rank's first layer x0 */
+    int ncell[3];      /* the cell grid of the whole box (as a context builds it) */
+} mdrl_slab;
+
+/* The slab of `rank` among `nranks` (layers split as evenly as possible, every rank at least one;
+ * nranks must not exceed the layer count).  Host only. */
+mdrl_status mdrl_slab_plan(const mdrl_params *p, int nranks, int rank, mdrl_slab *slab);
+
+/* Which particles (host arrays, any number) this rank owns (cell layer in [x0, x1)) and which of
+ * them it exports (layer x0); the cell of a particle is the one the GPU binning assigns.  owned
+ * and exported receive indices into x in increasing order; either may be NULL.  Host only. */
+mdrl_status mdrl_slab_select(const mdrl_params *p, const mdrl_slab *slab, int n, const float *x,
+                             int *owned, int *n_owned, int *exported, int *n_exported);
+
+/* One force evaluation (host or device arrays as mdrl_force_eval) of the units whose home cell
+ * lies in layers [home_x0, home_x1) (0 and ncell[0]: all), with the forces returned as the raw
+ * int64 accumulators (units of 2^-24 kcal/mol/A, F[3n]: x, y and z planes) so that partial
+ * results of several evaluations sum exactly.  MDRL_ACC_FIXED64 only. */
+mdrl_status mdrl_force_eval_fixed(mdrl_ctx *ctx, int n, const float *x, const float *y, const float *z,
+                                  const float *q, const int *type, int home_x0, int home_x1,
+                                  int64_t *F, mdrl_stats *stats);
+
 /* One force evaluation that allocates no memory; it has no counterpart in the reference.
  * For callers that cannot call cudaMalloc (a device owned by another allocator or memory pool,
  * a plugin host that forbids allocations, a loop that cannot pay for a first-use allocation):

@@ -55,6 +55,8 @@ def lib() -> C.CDLL:
         L.orc_force_direct64.argtypes = [C.POINTER(OrcSys), _D, C.POINTER(OrcStats)]
         L.orc_force_tables64.argtypes = [C.POINTER(OrcSys), _D, C.POINTER(OrcStats)]
         L.orc_force_split64.argtypes = [C.POINTER(OrcSys), C.c_int, C.c_int, _D, C.POINTER(OrcStats)]
+        L.orc_force_cells_fixed.argtypes = [C.POINTER(OrcSys), C.c_int, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_force_cells_fixed.restype = C.c_int64
         L.orc_force_cells_mt.argtypes = [C.POINTER(OrcSys), C.c_int, C.c_int, C.c_int, _F]
         L.orc_force_cells_mt.restype = C.c_int64
         L.orc_force_allpairs_mt.argtypes = [C.POINTER(OrcSys), C.c_int, _F]
@@ -134,6 +136,14 @@ class System:
         F = np.zeros((self.n, 3)); st = OrcStats()
         assert lib().orc_force_split64(C.byref(self.s), int(f32_diff), int(tables), _p(F, _D), C.byref(st)) >= 0
         return F, st.as_dict()
+
+    def force_cells_fixed(self, hbegin=0, hend=-1):
+        """Half-shell forces of the home cells [hbegin, hend) as int64 2^-24 fixed point, summed per
+        pair ((n, 3) int64, pair count)."""
+        F = np.zeros((self.n, 3), np.int64)
+        pairs = lib().orc_force_cells_fixed(C.byref(self.s), hbegin, hend, F.ctypes.data_as(C.POINTER(C.c_int64)))
+        assert pairs >= 0
+        return F, int(pairs)
 
     def force_cells_mt(self, nthreads=0, hbegin=0, hend=-1):
         F = np.zeros((self.n, 3), np.float32)

@@ -313,6 +313,32 @@ int orc_force_cells(const orc_sys *s, double *F, double *Fabs, int *counts, orc_
     return c.maxocc;
 }
 
+int64_t orc_force_cells_fixed(const orc_sys *s, int hbegin, int hend, int64_t *F) {
+    if (check_sys(s)) return -1;
+    Cells c;
+    build_cells(s, &c);
+    const int n = s->n;
+    memset(F, 0, sizeof(int64_t) * 3 * n);
+    const int ncells = c.nc[0] * c.nc[1] * c.nc[2];
+    if (hbegin < 0) hbegin = 0;
+    if (hend < 0 || hend > ncells) hend = ncells;
+    int64_t pairs = 0;
+    /* each pair's FP32 force as 2^-24 fixed point (round to nearest), summed in int64: the sum of
+     * any partition of the pairs over ranks is the same integer */
+    auto fix = [](float v) { return (int64_t)llrint((double)v * 16777216.0); };
+    for_each_candidate(s, c, hbegin, hend, [&](int i, int j) {
+        PairOut o;
+        if (!pair32(s, s->x[i], s->y[i], s->z[i], qof(s, i), s->type[i], s->x[j], s->y[j],
+                    s->z[j], qof(s, j), s->type[j], &o))
+            return;
+        ++pairs;
+        const int64_t fx = fix(o.fx), fy = fix(o.fy), fz = fix(o.fz);
+        F[3 * i] += fx; F[3 * i + 1] += fy; F[3 * i + 2] += fz;
+        F[3 * j] -= fx; F[3 * j + 1] -= fy; F[3 * j + 2] -= fz;
+    });
+    return pairs;
+}
+
 int orc_force_direct64(const orc_sys *s, double *F, orc_stats *st) {
     if (check_sys(s) || !s->pcoef64) return -1;
     Cells c;

@@ -92,6 +92,12 @@ int orc_force_cells(const orc_sys *s, double *F, double *Fabs, int *counts, orc_
 /* Same pair set, FP64 physics: A/r^14 + B/r^8 + ke*qi*qj/r^3 with exact differences. */
 int orc_force_direct64(const orc_sys *s, double *F, orc_stats *st);
 
+/* The half-shell traversal restricted to home cells [hbegin, hend) (hend < 0: all), each pair's
+ * FP32 force rounded to 2^-24 fixed point and summed in int64 into F[3n] (x, y, z interleaved):
+ * the checker of the spatial decomposition, whose ranks' partial sums must add up to the
+ * single-domain result exactly.  Returns the pair count. */
+int64_t orc_force_cells_fixed(const orc_sys *s, int hbegin, int hend, int64_t *F);
+
 /* Same pair set, FP64 evaluation of the FP32 table polynomials (index from the FP32 r2). */
 int orc_force_tables64(const orc_sys *s, double *F, orc_stats *st);
 

@@ -18,7 +18,7 @@ __all__ = [
     "cmodel_run", "md_evaluation_model", "Batch", "Replica", "Tile", "TUNE_RETIME", "PmeParams", "PATH_HALF_SHELL", "PATH_MIN_IMAGE",
     "PATH_ALL_IMAGES", "ACC_FIXED64", "ACC_FP32_ATOMIC", "ACC_KAHAN",
     "ARITH_FMA", "ARITH_SEPARATE", "EVAL_TABLE", "EVAL_DIRECT", "INT_VELOCITY_VERLET",
-    "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "FLAG_EXACT_DIFF", "TABLE_RAW",
+    "Slab", "slab_plan", "slab_select", "INT_EULER", "FLAG_ENERGY", "FLAG_PAIR_COUNTS", "FLAG_NO_PBC", "FLAG_EXACT_DIFF", "TABLE_RAW",
     "TABLE_BIN_LOCAL", "MAX_TYPES", "STATUS",
 ]
 
@@ -106,6 +106,34 @@ class Replica(C.Structure):
 PATH_HALF_SHELL, PATH_MIN_IMAGE, PATH_ALL_IMAGES = 0, 1, 2
 
 
+class Slab(C.Structure):
+    _fields_ = [("nranks", C.c_int), ("rank", C.c_int), ("x0", C.c_int), ("x1", C.c_int), ("halo_x", C.c_int),
+                ("import_from", C.c_int), ("export_to", C.c_int), ("ncell", C.c_int * 3)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ncell"}
+        d["ncell"] = tuple(self.ncell)
+        return d
+
+
+def slab_plan(params: "Params", nranks: int, rank: int) -> Slab:
+    """The slab of cell layers along x that `rank` owns (mdrl_slab_plan; host only)."""
+    s = Slab()
+    _check(lib().mdrl_slab_plan(C.byref(params), nranks, rank, C.byref(s)))
+    return s
+
+
+def slab_select(params: "Params", slab: Slab, x) -> tuple:
+    """(owned indices, exported indices) of the particles with x coordinates `x` (host only)."""
+    x = _f32(x)
+    n = x.shape[0]
+    owned, exported = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    no, ne = C.c_int(), C.c_int()
+    _check(lib().mdrl_slab_select(C.byref(params), C.byref(slab), n, _fp(x), _ip(owned), C.byref(no),
+                                  _ip(exported), C.byref(ne)))
+    return owned[:no.value], exported[:ne.value]
+
+
 def lib() -> C.CDLL:
     """The loaded libmdrl (raises when it has not been built)."""
     global _lib
@@ -124,6 +152,9 @@ def lib() -> C.CDLL:
     L.mdrl_fit_tables.argtypes = [st, st, st, st, st, _F]
     L.mdrl_fit_tables_bin_local.argtypes = [st, st, st, st, st, _F]
     L.mdrl_get_table_form.argtypes = [vp, _I]
+    L.mdrl_slab_plan.argtypes = [C.POINTER(Params), st, st, C.POINTER(Slab)]
+    L.mdrl_slab_select.argtypes = [C.POINTER(Params), C.POINTER(Slab), st, _F, _I, _I, _I, _I]
+    L.mdrl_force_eval_fixed.argtypes = [vp, st, _F, _F, _F, _F, _I, st, st, C.POINTER(C.c_int64), C.POINTER(Stats)]
     L.mdrl_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
     L.mdrl_destroy.argtypes = [vp]
     L.mdrl_set_tables.argtypes = [vp, st, st, st, st, st, _F, st]
@@ -169,7 +200,8 @@ def lib() -> C.CDLL:
                  "mdrl_batch_set_state", "mdrl_batch_step", "mdrl_batch_get_state",
                  "mdrl_batch_replica_stats", "mdrl_batch_time_force"):
         getattr(L, name).restype = st
-    for name in ("mdrl_fit_tables", "mdrl_fit_tables_bin_local", "mdrl_get_table_form", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
+    for name in ("mdrl_fit_tables", "mdrl_fit_tables_bin_local", "mdrl_get_table_form", "mdrl_slab_plan",
+                 "mdrl_slab_select", "mdrl_force_eval_fixed", "mdrl_create", "mdrl_destroy", "mdrl_set_tables",
                  "mdrl_get_tables", "mdrl_get_pair_coefficients", "mdrl_bin", "mdrl_force_eval",
                  "mdrl_force_eval_device", "mdrl_pair_eval", "mdrl_set_state", "mdrl_step",
                  "mdrl_get_state", "mdrl_cmodel_run", "mdrl_time_force", "mdrl_force_eval_static"):
@@ -383,6 +415,24 @@ class Context:
         _check(lib().mdrl_force_eval(self._h, n, _fp(x), _fp(y), _fp(z), _fp(q), _ip(t), _fp(fx),
                                      _fp(fy), _fp(fz), _ip(cnt), C.byref(st)))
         return np.stack([fx, fy, fz], axis=1), st.as_dict(), cnt
+
+    def force_fixed(self, x, y, z, q=None, type=None, home=None):
+        """Forces of the units whose home cell layer lies in home = (x0, x1) (None: all) as raw int64
+        2^-24 fixed point (mdrl_force_eval_fixed); returns ((n,3) int64, stats dict)."""
+        x = _f32(x)
+        n = x.shape[0]
+        y, z, q, t = _f32(y, n), _f32(z, n), _f32(q, n), _i32(type, n)
+        F = np.zeros((3, n), np.int64)
+        h0, h1 = home if home is not None else (0, self._ncell_x())
+        st = Stats()
+        _check(lib().mdrl_force_eval_fixed(self._h, n, _fp(x), _fp(y), _fp(z), _fp(q), _ip(t), h0, h1,
+                                           F.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(st)))
+        return np.ascontiguousarray(F.T), st.as_dict()
+
+    def _ncell_x(self) -> int:
+        p = self.params
+        return p.ncell[0] if p.ncell[0] > 0 else int(np.floor(np.float64(np.float32(p.box[0])) /
+                                                              np.float64(np.float32(p.cutoff))))
 
     def pair_eval(self, ref, nbr, type_ref=None, type_nbr=None):
         """Per-pair plugin: ref/nbr (n,4) float32 (x,y,z,q); returns (out (n,4), aux (n,2))."""

@@ -442,19 +442,22 @@ mdrl_status mdrl::prepare_force_kernel(force_fn fn, int device) {
 
 int mdrl::eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
 
+/* The force launch over units [unit0, unit0 + units) (units < 0: every unit). */
 static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra,
-                                     unsigned long long *F64, float *F32) {
+                                     unsigned long long *F64, float *F32, int unit0 = 0, int units = -1) {
     const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
     const bool prune = c->p.accum == MDRL_ACC_FIXED64 && c->tile.prune_steps;
     force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, fw, prune,
                              (c->p.flags & MDRL_FLAG_EXACT_DIFF) != 0);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
-    const int units = c->ncells * kHalfShellCells;
+    if (units < 0) units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
-    fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
-                                             c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr, nullptr,
-                                             tile_word(c->tile.steps_per_piece, c->tile.prune_steps), c->d_err);
+    if (units > 0)
+        fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
+                                                 c->p.ntypes, c->ke, n, F64, F32, c->d_cnt, c->d_unit, nullptr,
+                                                 nullptr, tile_word(c->tile.steps_per_piece, c->tile.prune_steps),
+                                                 c->d_err, unit0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;
@@ -691,6 +694,128 @@ extern "C" mdrl_status mdrl_force_eval(mdrl_ctx *c, int n, const float *x, const
     }
     MDRL_CUDA(cudaStreamSynchronize(c->stream));   /* the one synchronisation of the call */
     return force_eval_finish(c, st);
+}
+
+/* ---- spatial decomposition ------------------------------------------------------------------ */
+
+/* The cell grid a context builds for these parameters (setup_geometry), without a GPU. */
+static void grid_of(const mdrl_params *p, int nc[3], float edge[3]) {
+    const float rcf = (float)p->cutoff;
+    for (int d = 0; d < 3; ++d) {
+        const float L = (float)p->box[d];
+        const double ncd = p->ncell[d] > 0 ? (double)p->ncell[d] : std::floor((double)L / (double)rcf);
+        nc[d] = ncd > 65536.0 ? 65536 : (int)ncd;
+        edge[d] = nc[d] > 0 ? (float)((double)L / (double)nc[d]) : 0.0f;
+    }
+}
+
+extern "C" mdrl_status mdrl_slab_plan(const mdrl_params *p, int nranks, int rank, mdrl_slab *s) {
+    if (!p || !s) { set_error("mdrl_slab_plan: null argument"); return MDRL_ERR_INVALID_ARG; }
+    MDRL_TRY(validate_params(p));
+    int nc[3];
+    float edge[3];
+    grid_of(p, nc, edge);
+    if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3) {
+        set_error("mdrl_slab_plan: the half-shell traversal needs at least 3 cells per axis");
+        return MDRL_ERR_RANGE;
+    }
+    if (nranks < 1 || nranks > nc[0] || rank < 0 || rank >= nranks) {
+        set_error("mdrl_slab_plan: need 1 <= nranks <= cell layers along x and 0 <= rank < nranks");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    const int base = nc[0] / nranks, rem = nc[0] % nranks;
+    s->nranks = nranks;
+    s->rank = rank;
+    s->x0 = rank * base + std::min(rank, rem);
+    s->x1 = s->x0 + base + (rank < rem ? 1 : 0);
+    s->halo_x = s->x1 % nc[0];
+    s->import_from = (rank + 1) % nranks;
+    s->export_to = (rank + nranks - 1) % nranks;
+    for (int d = 0; d < 3; ++d) s->ncell[d] = nc[d];
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_slab_select(const mdrl_params *p, const mdrl_slab *s, int n, const float *x,
+                                        int *owned, int *n_owned, int *exported, int *n_exported) {
+    if (!p || !s || n < 0 || (n > 0 && !x)) { set_error("mdrl_slab_select: null or invalid argument"); return MDRL_ERR_INVALID_ARG; }
+    int nc[3];
+    float edge[3];
+    grid_of(p, nc, edge);
+    if (nc[0] != s->ncell[0] || s->x0 < 0 || s->x1 > nc[0] || s->x0 >= s->x1) {
+        set_error("mdrl_slab_select: the slab does not belong to these parameters");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    int no = 0, ne = 0;
+    for (int i = 0; i < n; ++i) {
+        /* the GPU binning's cell coordinate: floor(x / edge) in FP32, clamped into the grid */
+        const float f = std::floor(x[i] / edge[0]);
+        const int cx = !(f >= 0.0f) ? 0 : (f >= (float)nc[0] ? nc[0] - 1 : (int)f);
+        if (cx < s->x0 || cx >= s->x1) continue;
+        if (owned) owned[no] = i;
+        ++no;
+        if (cx == s->x0 && s->nranks > 1) {
+            if (exported) exported[ne] = i;
+            ++ne;
+        }
+    }
+    if (n_owned) *n_owned = no;
+    if (n_exported) *n_exported = ne;
+    return MDRL_OK;
+}
+
+extern "C" mdrl_status mdrl_force_eval_fixed(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,
+                                             const float *q, const int *type, int hx0, int hx1, int64_t *F,
+                                             mdrl_stats *st) {
+    if (!c || n < 0 || (n > 0 && (!x || !y || !z || !F))) {
+        set_error("mdrl_force_eval_fixed: null or invalid argument");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    if (c->p.accum != MDRL_ACC_FIXED64) {
+        set_error("mdrl_force_eval_fixed: needs MDRL_ACC_FIXED64");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    MDRL_CUDA(cudaSetDevice(c->p.device));
+    MDRL_TRY(ensure_capacity(c, n));
+    if (hx0 < 0 || hx1 > c->g.nc[0] || hx0 > hx1) {
+        set_error("mdrl_force_eval_fixed: home layers must satisfy 0 <= home_x0 <= home_x1 <= ncell[0]");
+        return MDRL_ERR_INVALID_ARG;
+    }
+    const size_t fb = sizeof(float) * (size_t)n;
+    const void *dx = n ? mapped(c, x) : nullptr, *dy = n ? mapped(c, y) : nullptr, *dz = n ? mapped(c, z) : nullptr;
+    const void *dq = (q && n) ? mapped(c, q) : nullptr, *dt = (type && n) ? mapped(c, type) : nullptr;
+    void *dF = n ? mapped(c, F) : nullptr;
+    const bool direct = n > 0 && dx && dy && dz && (!q || dq) && (!type || dt);
+    if (n > 0 && !direct) {
+        MDRL_CUDA(cudaMemcpyAsync(c->d_ux, x, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uy, y, fb, cudaMemcpyHostToDevice, c->stream));
+        MDRL_CUDA(cudaMemcpyAsync(c->d_uz, z, fb, cudaMemcpyHostToDevice, c->stream));
+        if (q) MDRL_CUDA(cudaMemcpyAsync(c->d_uq, q, fb, cudaMemcpyHostToDevice, c->stream));
+        if (type) MDRL_CUDA(cudaMemcpyAsync(c->d_ut, type, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+        dx = c->d_ux; dy = c->d_uy; dz = c->d_uz;
+        dq = q ? c->d_uq : nullptr;
+        dt = type ? c->d_ut : nullptr;
+    }
+    if (!dF && n > 0 && !c->d_Fscr64) MDRL_TRY(dalloc(&c->d_Fscr64, 3 * (size_t)c->cap));
+    long long *Fout = dF ? (long long *)dF : (long long *)c->d_Fscr64;
+    MDRL_CUDA(cudaMemsetAsync(c->d_tot, 0, sizeof(DevTotals), c->stream));
+    MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
+    MDRL_TRY(bin_user(c, n, (const float *)dx, (const float *)dy, (const float *)dz, (const float *)dq,
+                      (const int *)dt, 0, true, direct, true));
+    const int per_layer = c->g.nc[1] * c->g.nc[2] * kHalfShellCells;
+    const int units = (hx1 - hx0) * per_layer;
+    MDRL_TRY(launch_force_into(c, n, c->d_pos[0], c->d_type[0], false, c->d_F64, nullptr, hx0 * per_layer, units));
+    k_totals<<<1, 1024, 0, c->stream>>>(units, c->d_unit, 0, c->d_kepart, c->d_tot, 0);
+    if (n > 0) k_unsort_fixed<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_inv, c->d_F64, Fout);
+    MDRL_CUDA(cudaGetLastError());
+    MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
+    if (n > 0 && !dF)
+        MDRL_CUDA(cudaMemcpyAsync(F, c->d_Fscr64, 3 * sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    MDRL_CUDA(cudaStreamSynchronize(c->stream));
+    MDRL_TRY(check_device_errors(c));
+    c->have_state = false;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) != cudaSuccess) cudaGetLastError();
+    return read_stats(c, st, ms);
 }
 
 extern "C" mdrl_status mdrl_bin(mdrl_ctx *c, int n, const float *x, const float *y, const float *z,

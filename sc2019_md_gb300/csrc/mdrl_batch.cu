@@ -334,7 +334,7 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     fn<<<b->nitems, kBatchFT, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
                                                   c->p.ntypes, c->ke, b->ntot, F64, nullptr, c->d_cnt, c->d_unit,
-                                                  b->d_items, b->d_reps, tile_word(c->tile.steps_per_piece, c->tile.prune_steps), c->d_err);
+                                                  b->d_items, b->d_reps, tile_word(c->tile.steps_per_piece, c->tile.prune_steps), c->d_err, 0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
     return MDRL_OK;

@@ -66,7 +66,7 @@ struct BatchRep;
 struct BatchItem;
 typedef void (*force_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *,
                          int, float, int, unsigned long long *, float *, int *, UnitOut *,
-                         const BatchItem *, const BatchRep *, int, unsigned *);
+                         const BatchItem *, const BatchRep *, int, unsigned *, int);
 
 /* Work items (one per unit): the result slots k_totals sums. */
 inline int force_items(int ncells) { return ncells * kHalfShellCells; }
@@ -688,7 +688,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
         int ntypes, float ke, int n, unsigned long long *__restrict__ F64,
         float *__restrict__ F32, int *__restrict__ counts, UnitOut *__restrict__ uout,
         const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps, int tilecfg,
-        unsigned *__restrict__ err) {
+        unsigned *__restrict__ err, int unit0) {
     extern __shared__ float4 smem[];
     float4 *sIp = smem;
     float4 *sJp = sIp + kChunk;
@@ -702,7 +702,7 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int row = lane >> 3, col = lane & 7;
-    int unit = blockIdx.x, coff = 0;
+    int unit = blockIdx.x + unit0, coff = 0;   /* unit0: first unit of a restricted home range */
     bool cell_pair = false, use_wrap = false;
     Geom gb;
     if (BATCH) {

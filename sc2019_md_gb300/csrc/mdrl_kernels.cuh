@@ -526,6 +526,18 @@ static __global__ void k_unsort_inv(int n, const int *__restrict__ inv, const un
     if (cnt_u) cnt_u[id] = cnt_s[k];
 }
 
+/* The raw int64 accumulators in user order (x, y, z planes of n), for partial evaluations that
+ * are summed exactly (spatial decomposition). */
+static __global__ void k_unsort_fixed(int n, const int *__restrict__ inv, const unsigned long long *__restrict__ F64,
+                                      long long *__restrict__ out) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const int k = inv[id];
+    out[id] = (long long)F64[k];
+    out[(size_t)n + id] = (long long)F64[(size_t)n + k];
+    out[2 * (size_t)n + id] = (long long)F64[2 * (size_t)n + k];
+}
+
 /* ------------------------------------------------------------------------------------------ */
 /* Motion update on cell-sorted state.                                                         */
 

@@ -319,7 +319,7 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
                                  (int)force_smem_bytes(MDRL_MAX_TYPES, true, 8)));
     fn<<<nc * kHalfShellCells, kFT, smem, st>>>(d_pos, d_type, d_start, g, tab, d_pcoef, p->ntypes,
                                                 (float)p->coulomb_k, n, d_F64, nullptr, nullptr, d_unit, nullptr,
-                                                nullptr, tile_word(kStepsPerPiece, 0), d_err);
+                                                nullptr, tile_word(kStepsPerPiece, 0), d_err, 0);
     k_totals<<<1, 1024, 0, st>>>(force_items(nc), d_unit, 0, nullptr, d_tot, 0);
     if (n > 0)
         k_unsort<<<grid, blk, 0, st>>>(n, d_id, d_F64, nullptr, nullptr, fx, fy, fz, nullptr);
