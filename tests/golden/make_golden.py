@@ -1,7 +1,7 @@
 """Generate the golden fixtures of tests/golden/ from the reference project.
 
-Run where the reference tree is mounted (MDRL_REFERENCE, default /root/reference):
-    python tests/golden/make_golden.py
+Run where the reference tree is mounted, naming it in MDRL_REFERENCE:
+    MDRL_REFERENCE=<reference project root> python tests/golden/make_golden.py
 Every fixture is derived from the reference's own files or from the unmodified reference C model
 (oracle/_ref/cmodel_ref, built by oracle/build_ref.sh); nothing here is read at test time
 except the .npz/.txt files it writes.
@@ -48,7 +48,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path(os.environ.get("MDRL_REFERENCE", "/root/reference"))
+if not os.environ.get("MDRL_REFERENCE"):
+    raise SystemExit("set MDRL_REFERENCE to the reference project's root")
+REF = Path(os.environ["MDRL_REFERENCE"])
 SC = REF / "Range_Limited_demo" / "SourceCode"
 MS = SC / "MatlabScripts"
 HDL = SC / "OpenCL_HDL_Lib" / "HDL_Source"

@@ -19,8 +19,9 @@ import oracle
 from sc2019_md_gb300 import formats as F
 from helpers import GOLDEN, kat2_positions
 
-REF = Path(os.environ.get("MDRL_REFERENCE", "/root/reference"))
-DHFR = REF / "Range_Limited_demo" / "SourceCode" / "MatlabScripts" / "DHFR_23k_Input_Dataset"
+# the reference project's tree, when a caller names it (MDRL_REFERENCE); the DHFR checks skip without it
+REF = Path(os.environ["MDRL_REFERENCE"]) if os.environ.get("MDRL_REFERENCE") else None
+DHFR = (REF / "Range_Limited_demo" / "SourceCode" / "MatlabScripts" / "DHFR_23k_Input_Dataset") if REF else Path("/nonexistent")
 
 
 def _sha(text: str) -> str:
