@@ -4,6 +4,7 @@ the toolkit that built the library."""
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -65,10 +66,19 @@ def build(force: bool = False, ptxas_verbose: bool = False, out_dir: Path | None
     """Compile every CUDA/C++ translation unit and link libmdrl.so; returns its path.  `out_dir`
     and `defines` (-D flags) build a variant elsewhere (tuning sweeps)."""
     out = OUT if out_dir is None else Path(out_dir)
-    lib = out / "libmdrl.so"
     if out_dir is None and not defines and not force and not ptxas_verbose and up_to_date():
         return LIB
     out.mkdir(parents=True, exist_ok=True)
+    # concurrent builds into one folder (processes started together) run one at a time
+    with open(out / ".build.lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if out_dir is None and not defines and not force and not ptxas_verbose and up_to_date():
+            return LIB
+        return _build_locked(out, ptxas_verbose, defines)
+
+
+def _build_locked(out: Path, ptxas_verbose: bool, defines: tuple) -> Path:
+    lib = out / "libmdrl.so"
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         results = list(ex.map(lambda s: _compile(s, ptxas_verbose, out, defines), srcs))

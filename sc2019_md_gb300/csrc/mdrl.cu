@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "mdrl_ctx.cuh"
+#include "mdrl_force_warp.cuh"
 
 using namespace mdrl;
 
@@ -368,7 +369,7 @@ static mdrl_status ensure_cells(mdrl_ctx *c) {
     c->ncells = c->g.nc[0] * c->g.nc[1] * c->g.nc[2];
     MDRL_TRY(dalloc(&c->d_count, c->ncells));
     MDRL_TRY(dalloc(&c->d_start, c->ncells + 1));
-    MDRL_TRY(dalloc(&c->d_unit, (size_t)c->ncells * kHalfShellCells));
+    MDRL_TRY(dalloc(&c->d_unit, (size_t)c->ncells * kHalfShellCells * kMaxItemGroups));
     return MDRL_OK;
 }
 
@@ -442,16 +443,38 @@ mdrl_status mdrl::prepare_force_kernel(force_fn fn, int device) {
 
 int mdrl::eff_order(const mdrl_ctx *c) { return c->p.eval == MDRL_EVAL_DIRECT ? 0 : c->order; }
 
+/* Result slots of a force launch over `units` units: one per CTA (the warp-item kernel runs
+ * steps_per_piece i-tile groups per unit). */
+static int force_slots(const mdrl_ctx *c, int units) {
+    return c->tile.warps_per_cta == 1 ? units * c->tile.steps_per_piece : units;
+}
+
 /* The force launch over units [unit0, unit0 + units) (units < 0: every unit). */
 static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, const int *type, bool extra,
                                      unsigned long long *F64, float *F32, int unit0 = 0, int units = -1) {
+    if (units < 0) units = c->ncells * kHalfShellCells;
+    if (c->tile.warps_per_cta == 1) {
+        /* one warp per (unit, i-tile group); fixed point only (set_tile checks) */
+        const bool exact = (c->p.flags & MDRL_FLAG_EXACT_DIFF) != 0;
+        force_fn fn = exact ? pick_force_warp_set<0, kDiffExact>(eff_order(c), false, extra)
+                            : pick_force_warp_set<0, kDiffShift>(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra);
+        MDRL_TRY(prepare_force_kernel(fn, c->p.device));
+        const int items = force_slots(c, units);
+        MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
+        if (items > 0)
+            fn<<<items, 32, force_warp_smem_bytes(c->p.ntypes), c->stream>>>(
+                pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, n, F64, F32, c->d_cnt,
+                c->d_unit, nullptr, nullptr, c->tile.steps_per_piece, c->d_err, unit0);
+        MDRL_CUDA(cudaGetLastError());
+        MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
+        return MDRL_OK;
+    }
     const int fw = c->p.accum == MDRL_ACC_FIXED64 ? c->tile.warps_per_cta : kFW;
     const bool prune = c->p.accum == MDRL_ACC_FIXED64 && c->tile.prune_steps;
     force_fn fn = pick_force(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->p.accum, fw, prune,
                              (c->p.flags & MDRL_FLAG_EXACT_DIFF) != 0);
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, fw);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
-    if (units < 0) units = c->ncells * kHalfShellCells;
     MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
     if (units > 0)
         fn<<<units, fw * 32, smem, c->stream>>>(pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef,
@@ -588,7 +611,7 @@ static mdrl_status force_eval_enqueue(mdrl_ctx *c, int n, const float *x, const 
     const bool energy = (c->p.flags & MDRL_FLAG_ENERGY) != 0;
     MDRL_TRY(pme_enqueue(c, n, c->d_pos[0], c->d_F64, c->d_F32, energy));
     MDRL_TRY(bonded_enqueue(c, n, c->d_pos[0], c->d_id[0], c->d_F64, c->d_F32, energy));
-    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, 0, c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_slots(c, force_items(c->ncells)), c->d_unit, 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (energy) MDRL_TRY(pme_add_energy(c, n));
     if (energy) MDRL_TRY(bonded_add_energy(c, n));
@@ -804,7 +827,7 @@ extern "C" mdrl_status mdrl_force_eval_fixed(mdrl_ctx *c, int n, const float *x,
     const int per_layer = c->g.nc[1] * c->g.nc[2] * kHalfShellCells;
     const int units = (hx1 - hx0) * per_layer;
     MDRL_TRY(launch_force_into(c, n, c->d_pos[0], c->d_type[0], false, c->d_F64, nullptr, hx0 * per_layer, units));
-    k_totals<<<1, 1024, 0, c->stream>>>(units, c->d_unit, 0, c->d_kepart, c->d_tot, 0);
+    k_totals<<<1, 1024, 0, c->stream>>>(force_slots(c, units), c->d_unit, 0, c->d_kepart, c->d_tot, 0);
     if (n > 0) k_unsort_fixed<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_inv, c->d_F64, Fout);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaEventRecord(c->ev1, c->stream));
@@ -1031,7 +1054,7 @@ extern "C" mdrl_status mdrl_set_state(mdrl_ctx *c, int n, const float *x, const 
     MDRL_TRY(bonded_enqueue(c, n, c->d_pos[0], c->d_id[0], c->d_F64, c->d_F32, extra));
     k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, c->d_F32, c->d_mt, 0,
                                                 c->d_kepart);
-    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_slots(c, force_items(c->ncells)), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
     if (extra) MDRL_TRY(bonded_add_energy(c, n));
@@ -1069,7 +1092,7 @@ static mdrl_status enqueue_step(mdrl_ctx *c, bool extra) {
     if (vv || extra)
         k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[b], c->d_type[b], c->d_F64, c->d_F32, c->d_mt,
                                                     vv ? 1 : 0, extra ? c->d_kepart : nullptr);
-    k_totals<<<1, 1024, 0, c->stream>>>(force_items(c->ncells), c->d_unit, extra ? nblk(n, 256) : 0,
+    k_totals<<<1, 1024, 0, c->stream>>>(force_slots(c, force_items(c->ncells)), c->d_unit, extra ? nblk(n, 256) : 0,
                                        c->d_kepart, c->d_tot, extra ? 1 : 0);
     if (extra) MDRL_TRY(pme_add_energy(c, n));
     if (extra) MDRL_TRY(bonded_add_energy(c, n));
@@ -1157,9 +1180,21 @@ extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z,
 /* ---- tiles and the autotuner --------------------------------------------------------------- */
 
 static mdrl_status check_tile(const mdrl_tile *t, bool allow8, bool allow_prune) {
+    if (t && t->warps_per_cta == 1) {
+        /* the warp-item kernel: steps_per_piece = i-tile groups per unit; it always prunes */
+        if (t->steps_per_piece < 1 || t->steps_per_piece > kMaxItemGroups || t->prune_steps != 1) {
+            set_error("tile: one warp per item takes 1..4 i-tile groups (steps_per_piece) and prune_steps 1");
+            return MDRL_ERR_INVALID_ARG;
+        }
+        if (!allow8) {
+            set_error("tile: one warp per item needs MDRL_ACC_FIXED64 (and no batch)");
+            return MDRL_ERR_INVALID_ARG;
+        }
+        return MDRL_OK;
+    }
     if (!t || (t->warps_per_cta != 4 && t->warps_per_cta != 8) || t->steps_per_piece < 1 ||
         t->steps_per_piece > 32 || (t->prune_steps != 0 && t->prune_steps != 1)) {
-        set_error("tile: warps_per_cta must be 4 or 8, steps_per_piece in 1..32, prune_steps 0 or 1");
+        set_error("tile: warps_per_cta must be 1, 4 or 8, steps_per_piece in 1..32, prune_steps 0 or 1");
         return MDRL_ERR_INVALID_ARG;
     }
     if (t->warps_per_cta == 8 && !allow8) {
@@ -1209,7 +1244,9 @@ static void tune_load_locked() {
     int w, s, pr;
     float ms;
     while (in >> key >> w >> s >> pr >> ms)
-        if ((w == 4 || w == 8) && s >= 1 && s <= 32 && (pr == 0 || pr == 1)) g_tune[key] = mdrl_tile{w, s, pr};
+        if (((w == 4 || w == 8) && s >= 1 && s <= 32 && (pr == 0 || pr == 1)) ||
+            (w == 1 && s >= 1 && s <= kMaxItemGroups && pr == 1))
+            g_tune[key] = mdrl_tile{w, s, pr};
 }
 
 static void tune_store_locked(const std::string &key, const mdrl_tile &t, float ms) {
@@ -1293,6 +1330,13 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
                         def_ms = ms;
                     if (ms < pick_ms) { pick_ms = ms; pick = t; }
                 }
+        if (c->p.accum == MDRL_ACC_FIXED64)
+            for (int grp = 1; grp <= 3; ++grp) {   /* one warp per (unit, i-tile group) */
+                const mdrl_tile t = {1, grp, 1};
+                float ms;
+                MDRL_TRY(time_tile(t, &ms));
+                if (ms < pick_ms) { pick_ms = ms; pick = t; }
+            }
         tune_store(key, pick, pick_ms);
     }
     MDRL_TRY(set_tile(c, &pick, true));

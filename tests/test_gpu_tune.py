@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 SUM_TOL = 2e-6
 FIX_ABS = 64 * 2.0 ** -24
-CANDIDATES = {(w, s, p) for w in (4, 8) for s in (3, 4, 6, 8, 12) for p in (0, 1)}
+CANDIDATES = {(w, s, p) for w in (4, 8) for s in (3, 4, 6, 8, 12) for p in (0, 1)} | {(1, g, 1) for g in (1, 2, 3)}
 
 
 @pytest.fixture(scope="module")
@@ -31,7 +31,8 @@ def sysm():
     return systems.small_ljc(3000, 37.5, 12.0, seed=21)     # 3 x 3 x 3 cells, ~110 per cell
 
 
-@pytest.mark.parametrize("tile", [(4, 3, 0), (4, 12, 1), (8, 6, 1), (8, 1, 0), (4, 32, 1), (4, 6, 1)])
+@pytest.mark.parametrize("tile", [(4, 3, 0), (4, 12, 1), (8, 6, 1), (8, 1, 0), (4, 32, 1), (4, 6, 1),
+                                  (1, 1, 1), (1, 2, 1), (1, 4, 1)])
 @pytest.mark.parametrize("grid", ["3 cells", "4 cells"])
 @pytest.mark.parametrize("exact", [False, True])
 def test_tile_parity_and_reproducibility(sysm, tile, grid, exact):
@@ -143,5 +144,13 @@ def test_tile_validation(sysm):
             ctx.set_tile(4, 6, 2)
         with pytest.raises(m.MdrlError):
             ctx.set_tile(4, 6, 1)                   # pruned kernels exist for fixed point only
+        with pytest.raises(m.MdrlError):
+            ctx.set_tile(1, 1, 1)                   # one warp per item: fixed point only
         ctx.set_tile(4, 12)
         assert ctx.tile() == (4, 12, 0)
+    with m.Context(sysm.params()) as ctx:
+        for bad in ((1, 0, 1), (1, 5, 1), (1, 2, 0)):
+            with pytest.raises(m.MdrlError):
+                ctx.set_tile(*bad)
+        ctx.set_tile(1, 3, 1)
+        assert ctx.tile() == (1, 3, 1)
