@@ -256,13 +256,17 @@ def clustered(n_big: int, n_rest: int, L: float = 37.5, seed: int = 5):
     return dataclasses.replace(base, pos=pos, vel=np.zeros_like(pos), q=q, type=t)
 
 
-def test_large_cell_chunked_sort_matches_oracle():
+@pytest.mark.parametrize("tile", [None, (1, 1, 1), (1, 3, 1)])
+def test_large_cell_chunked_sort_matches_oracle(tile):
     """A cell of 3,000 particles (above the 1,024 of the one-pass sort): the binning order equals
-    the oracle's and the forces, counts and pair total keep parity."""
+    the oracle's and the forces, counts and pair total keep parity, with the default tile and with
+    one warp per item (whose j cell is taken 256 particles at a time)."""
     sysm = clustered(3000, 1500)
     pos = sysm.pos
     p = sysm.params(table_bins=512, flags=m.FLAG_ENERGY)
     with m.Context(p) as ctx:
+        if tile is not None:
+            ctx.set_tile(*tile)
         cell_of, count, order = ctx.bin(pos[:, 0], pos[:, 1], pos[:, 2])
         assert count.max() >= 3000
         F, st, cnt = ctx.force(pos[:, 0], pos[:, 1], pos[:, 2], sysm.q, sysm.type, counts=True)

@@ -119,9 +119,9 @@ def test_force_small_ljc(order, bins, arith, exact):
     _check_force(sysm, p)
 
 
-@pytest.mark.parametrize("accum", [m.ACC_FIXED64, m.ACC_FP32_ATOMIC])
+@pytest.mark.parametrize("accum,tile", [(m.ACC_FIXED64, None), (m.ACC_FIXED64, (1, 2, 1)), (m.ACC_FP32_ATOMIC, None)])
 @pytest.mark.parametrize("which", ["lj1728", "ljc92k"])
-def test_force_error_bound(which, accum):
+def test_force_error_bound(which, accum, tile):
     """The stated accuracy: with the exact-difference rule and the library's bin-local order-2
     tables (512 bins), the GPU forces are within 1e-5 of the FP64 direct oracle in the primary
     norm, max_i |dF_i| / rms_j |F_j| (median per-particle relative error within 1e-6), for the
@@ -129,7 +129,7 @@ def test_force_error_bound(which, accum):
     bit-equal to the oracle's exact-rule datapath."""
     sysm = getattr(systems, which)()
     p = sysm.params(table_order=2, table_bins=512, flags=m.FLAG_EXACT_DIFF, accum=accum)
-    F, Fo, o = _check_force(sysm, p)
+    F, Fo, o = _check_force(sysm, p, tile=tile)
     F64, _ = o.force_direct64()
     emax, emed = force_err(F, F64)
     assert emax <= 1e-5, emax
@@ -224,7 +224,7 @@ def test_edge_cases():
 
 
 @pytest.mark.parametrize("ncell,L,ndimers,seed", [(5, 50.5, 600, 5), (3, 31.5, 300, 6)])
-@pytest.mark.parametrize("tile", [None, (4, 6, 1)])
+@pytest.mark.parametrize("tile", [None, (4, 6, 1), (1, 1, 1)])
 def test_cutoff_boundary_pairs(ncell, L, ndimers, seed, tile):
     """Dimers whose r2 lies exactly on rc2 or one ulp either side under the reference's rounding,
     chosen so that a fused multiply-add in r2 would decide them the other way (hundreds of such
@@ -240,7 +240,7 @@ def test_cutoff_boundary_pairs(ncell, L, ndimers, seed, tile):
     _check_force(sysm, sysm.params(table_bins=512, flags=m.FLAG_ENERGY), tile=tile)
 
 
-@pytest.mark.parametrize("tile", [None, (4, 6, 1), (8, 4, 1)])
+@pytest.mark.parametrize("tile", [None, (4, 6, 1), (8, 4, 1), (1, 1, 1), (1, 2, 1)])
 @pytest.mark.parametrize("exact", [False, True])
 def test_full_size_ljc92k_counts_and_forces(tile, exact):
     """The 92,224-atom LJ+Coulomb system at full size, with the default tile and with pruned
@@ -263,9 +263,14 @@ def test_full_size_ljc1m_pairs_and_reproducibility():
         F2, _, _ = ctx.force(x, y, z, sysm.q, sysm.type)
         ctx.set_tile(4, 6, 1)
         _, st_pruned, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        ctx.set_tile(1, 1, 1)
+        Fw1, st_warp, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        Fw2, _, _ = ctx.force(x, y, z, sysm.q, sysm.type)
         o = oracle_from_ctx(ctx, sysm)
     _, pairs = o.force_cells_mt(0)
     assert st["pairs"] == pairs
     assert st_pruned["pairs"] == pairs
+    assert st_warp["pairs"] == pairs
+    assert np.array_equal(Fw1.view(np.uint32), Fw2.view(np.uint32))
     assert np.array_equal(F1.view(np.uint32), F2.view(np.uint32))
     assert np.isfinite(F1).all()
