@@ -1179,15 +1179,15 @@ extern "C" mdrl_status mdrl_get_state(mdrl_ctx *c, float *x, float *y, float *z,
 
 /* ---- tiles and the autotuner --------------------------------------------------------------- */
 
-static mdrl_status check_tile(const mdrl_tile *t, bool allow8, bool allow_prune) {
+static mdrl_status check_tile(const mdrl_tile *t, bool allow8, bool allow_prune, bool allow_warp) {
     if (t && t->warps_per_cta == 1) {
         /* the warp-item kernel: steps_per_piece = i-tile groups per unit; it always prunes */
         if (t->steps_per_piece < 1 || t->steps_per_piece > kMaxItemGroups || t->prune_steps != 1) {
             set_error("tile: one warp per item takes 1..4 i-tile groups (steps_per_piece) and prune_steps 1");
             return MDRL_ERR_INVALID_ARG;
         }
-        if (!allow8) {
-            set_error("tile: one warp per item needs MDRL_ACC_FIXED64 (and no batch)");
+        if (!allow_warp) {
+            set_error("tile: one warp per item needs MDRL_ACC_FIXED64");
             return MDRL_ERR_INVALID_ARG;
         }
         return MDRL_OK;
@@ -1217,8 +1217,8 @@ static void drop_graphs(mdrl_ctx *c) {
 }
 
 namespace mdrl {
-mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8) {
-    MDRL_TRY(check_tile(t, allow8, c->p.accum == MDRL_ACC_FIXED64));
+mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8, bool allow_warp) {
+    MDRL_TRY(check_tile(t, allow8, c->p.accum == MDRL_ACC_FIXED64, allow_warp));
     if (t->warps_per_cta != c->tile.warps_per_cta || t->steps_per_piece != c->tile.steps_per_piece ||
         t->prune_steps != c->tile.prune_steps) {
         MDRL_CUDA(cudaSetDevice(c->p.device));
@@ -1284,7 +1284,7 @@ static const int kTuneSpp[] = {3, 4, 6, 8, 12};
 
 extern "C" mdrl_status mdrl_set_tile(mdrl_ctx *c, const mdrl_tile *t) {
     if (!c || !t) { set_error("mdrl_set_tile: null argument"); return MDRL_ERR_INVALID_ARG; }
-    return set_tile(c, t, c->p.accum == MDRL_ACC_FIXED64);
+    return set_tile(c, t, c->p.accum == MDRL_ACC_FIXED64, c->p.accum == MDRL_ACC_FIXED64);
 }
 
 extern "C" mdrl_status mdrl_get_tile(mdrl_ctx *c, mdrl_tile *t) {
@@ -1302,7 +1302,7 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
     snprintf(buf, sizeof buf, "ctx-%dx%dx%d-p%d-", c->g.nc[0], c->g.nc[1], c->g.nc[2], ppc8);
     const std::string key = std::string(buf) + tune_key_common(c);
     auto time_tile = [&](const mdrl_tile &t, float *ms) -> mdrl_status {
-        MDRL_TRY(set_tile(c, &t, true));
+        MDRL_TRY(set_tile(c, &t, true, true));
         float v[5];
         for (int r = 0; r < 5; ++r) MDRL_TRY(mdrl_time_force(c, &v[r]));
         std::sort(v, v + 5);
@@ -1339,7 +1339,7 @@ extern "C" mdrl_status mdrl_autotune(mdrl_ctx *c, int flags, mdrl_tile *best, fl
             }
         tune_store(key, pick, pick_ms);
     }
-    MDRL_TRY(set_tile(c, &pick, true));
+    MDRL_TRY(set_tile(c, &pick, true, true));
     if (best) *best = pick;
     if (best_ms) *best_ms = pick_ms;
     if (default_ms) *default_ms = def_ms;

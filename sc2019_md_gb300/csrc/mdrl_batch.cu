@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "mdrl_ctx.cuh"
+#include "mdrl_force_warp.cuh"
 
 using namespace mdrl;
 
@@ -91,8 +92,13 @@ __global__ void k_bkick_drift_bin(int n, float4 *__restrict__ pos, float4 *__res
 
 /* Per-replica totals of the last force evaluation (its items, in item order) and, when vel is
  * given, its kinetic energy (particles in cell order); one CTA per replica, fixed order. */
+/* With a one-warp-per-item tile the slots are laid out as [the other items' CTAs][G slots per
+ * half-shell item]; item_begin2 / rep_items2 then list a replica's half-shell items (positions in
+ * that list), whose G slots follow slot0 (nullptr: a single list). */
 __global__ void __launch_bounds__(128) k_rep_totals(const int *__restrict__ item_begin,
                                                     const int *__restrict__ rep_items,
+                                                    const int *__restrict__ item_begin2,
+                                                    const int *__restrict__ rep_items2, int slot0, int G,
                                                     const UnitOut *__restrict__ uout,
                                                     const BatchRep *__restrict__ reps,
                                                     const float4 *__restrict__ vel,
@@ -108,6 +114,12 @@ __global__ void __launch_bounds__(128) k_rep_totals(const int *__restrict__ item
         a += u.e_lj; b += u.e_coul; c += u.virial;
         p += u.pairs; q += u.below;
     }
+    if (item_begin2)
+        for (int e = G * item_begin2[r] + t; e < G * item_begin2[r + 1]; e += 128) {
+            const UnitOut u = uout[slot0 + G * rep_items2[e / G] + e % G];
+            a += u.e_lj; b += u.e_coul; c += u.virial;
+            p += u.pairs; q += u.below;
+        }
     if (vel) {
         const BatchRep &rp = reps[r];
         for (int e = t; e < rp.n; e += 128) {
@@ -146,6 +158,11 @@ struct mdrl_batch {
     BatchRep *d_reps = nullptr;
     BatchItem *d_items = nullptr;
     int *d_rep_of = nullptr, *d_item_begin = nullptr, *d_rep_items = nullptr;
+    /* the same work split for one-warp-per-item tiles: half-shell items (warp kernel) and the
+     * others (the CTA kernel), each in cost order, with per-replica lists */
+    int n_hs = 0, n_ot = 0;
+    BatchItem *d_items_hs = nullptr, *d_items_ot = nullptr;
+    int *d_begin_hs = nullptr, *d_list_hs = nullptr, *d_begin_ot = nullptr, *d_list_ot = nullptr;
     RepTotals *d_reptot = nullptr;
     bool have_eval = false;  /* the unit outputs hold a force evaluation */
 };
@@ -198,6 +215,8 @@ extern "C" mdrl_status mdrl_batch_destroy(mdrl_batch *b) {
     }
     dfree(&b->d_reps); dfree(&b->d_items); dfree(&b->d_rep_of); dfree(&b->d_item_begin);
     dfree(&b->d_rep_items); dfree(&b->d_reptot);
+    dfree(&b->d_items_hs); dfree(&b->d_items_ot); dfree(&b->d_begin_hs); dfree(&b->d_list_hs);
+    dfree(&b->d_begin_ot); dfree(&b->d_list_ot);
     if (b->c) mdrl_destroy(b->c);
     delete b;
     return MDRL_OK;
@@ -290,6 +309,22 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
         std::vector<int> fill(bt->item_begin.begin(), bt->item_begin.end() - 1);
         for (int k = 0; k < bt->nitems; ++k) bt->rep_items[fill[bt->items[k].rep]++] = k;
     }
+    /* the split for one-warp-per-item tiles (cost order kept within each list) */
+    std::vector<BatchItem> items_hs, items_ot;
+    for (const BatchItem &it : bt->items) (hrep[it.rep].path == kPathHalfShell ? items_hs : items_ot).push_back(it);
+    bt->n_hs = (int)items_hs.size();
+    bt->n_ot = (int)items_ot.size();
+    auto rep_lists = [&](const std::vector<BatchItem> &v, std::vector<int> &begin, std::vector<int> &list) {
+        begin.assign(nrep + 1, 0);
+        for (const BatchItem &it : v) begin[it.rep + 1]++;
+        for (int r = 0; r < nrep; ++r) begin[r + 1] += begin[r];
+        list.assign(v.size(), 0);
+        std::vector<int> fill(begin.begin(), begin.end() - 1);
+        for (size_t k = 0; k < v.size(); ++k) list[fill[v[k].rep]++] = (int)k;
+    };
+    std::vector<int> begin_hs, list_hs, begin_ot, list_ot;
+    rep_lists(items_hs, begin_hs, list_hs);
+    rep_lists(items_ot, begin_ot, list_ot);
     /* the context carries the force field; its own box is the first replica's (never used) */
     mdrl_params pc = *p;
     for (int d = 0; d < 3; ++d) { pc.box[d] = reps[0].box[d]; pc.ncell[d] = 0; }
@@ -301,7 +336,8 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
     c->ncells = bt->ncells;
     if ((s = dalloc(&c->d_count, (size_t)bt->ncells)) != MDRL_OK) return fail(s);
     if ((s = dalloc(&c->d_start, (size_t)bt->ncells + 1)) != MDRL_OK) return fail(s);
-    if ((s = dalloc(&c->d_unit, (size_t)bt->nitems)) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&c->d_unit, std::max((size_t)bt->nitems, (size_t)bt->n_ot + (size_t)bt->n_hs * kMaxItemGroups))) != MDRL_OK)
+        return fail(s);
     if ((s = ensure_capacity(c, bt->ntot)) != MDRL_OK) return fail(s);
     std::vector<int> rep_of(bt->ntot);
     for (int r = 0; r < nrep; ++r)
@@ -312,11 +348,23 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
     if ((s = dalloc(&bt->d_item_begin, (size_t)nrep + 1)) != MDRL_OK) return fail(s);
     if ((s = dalloc(&bt->d_rep_items, (size_t)bt->nitems)) != MDRL_OK) return fail(s);
     if ((s = dalloc(&bt->d_reptot, (size_t)nrep)) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_items_hs, std::max<size_t>(1, items_hs.size()))) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_items_ot, std::max<size_t>(1, items_ot.size()))) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_begin_hs, (size_t)nrep + 1)) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_begin_ot, (size_t)nrep + 1)) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_list_hs, std::max<size_t>(1, list_hs.size()))) != MDRL_OK) return fail(s);
+    if ((s = dalloc(&bt->d_list_ot, std::max<size_t>(1, list_ot.size()))) != MDRL_OK) return fail(s);
     cudaError_t e = cudaMemcpy(bt->d_reps, bt->reps.data(), sizeof(BatchRep) * nrep, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_items, bt->items.data(), sizeof(BatchItem) * bt->nitems, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_rep_of, rep_of.data(), sizeof(int) * bt->ntot, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_item_begin, bt->item_begin.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_rep_items, bt->rep_items.data(), sizeof(int) * bt->nitems, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bt->n_hs) e = cudaMemcpy(bt->d_items_hs, items_hs.data(), sizeof(BatchItem) * bt->n_hs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bt->n_ot) e = cudaMemcpy(bt->d_items_ot, items_ot.data(), sizeof(BatchItem) * bt->n_ot, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_begin_hs, begin_hs.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_begin_ot, begin_ot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bt->n_hs) e = cudaMemcpy(bt->d_list_hs, list_hs.data(), sizeof(int) * bt->n_hs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bt->n_ot) e = cudaMemcpy(bt->d_list_ot, list_ot.data(), sizeof(int) * bt->n_ot, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         set_error(std::string("mdrl_batch_create: ") + cudaGetErrorString(e));
         return fail(MDRL_ERR_CUDA);
@@ -325,9 +373,36 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
     return MDRL_OK;
 }
 
+/* Result slots of a batch force launch (one per CTA). */
+static int batch_slots(const mdrl_batch *b) {
+    return b->c->tile.warps_per_cta == 1 ? b->n_ot + b->n_hs * b->c->tile.steps_per_piece : b->nitems;
+}
+
 static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const int *type, bool extra,
                                       unsigned long long *F64) {
     mdrl_ctx *c = b->c;
+    if (c->tile.warps_per_cta == 1) {
+        /* the replicas with fewer than 3 cells per axis in the CTA kernel (default tile), then the
+         * half-shell units one warp per (unit, i-tile group) */
+        const bool sep = c->p.arith == MDRL_ARITH_SEPARATE;
+        force_fn fo = pick_force_batch(eff_order(c), sep, extra, false);
+        force_fn fw = pick_force_warp_batch(eff_order(c), sep, extra);
+        MDRL_TRY(prepare_force_kernel(fo, c->p.device));
+        MDRL_TRY(prepare_force_kernel(fw, c->p.device));
+        const int G = c->tile.steps_per_piece;
+        MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
+        if (b->n_ot)
+            fo<<<b->n_ot, kBatchFT, force_smem_bytes(c->p.ntypes, extra, kBatchFT / 32), c->stream>>>(
+                pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
+                c->d_cnt, c->d_unit, b->d_items_ot, b->d_reps, tile_word(kStepsPerPiece, 0), c->d_err, 0);
+        if (b->n_hs)
+            fw<<<b->n_hs * G, 32, force_warp_smem_bytes(c->p.ntypes), c->stream>>>(
+                pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
+                c->d_cnt, c->d_unit + b->n_ot, b->d_items_hs, b->d_reps, G, c->d_err, 0);
+        MDRL_CUDA(cudaGetLastError());
+        MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
+        return MDRL_OK;
+    }
     force_fn fn = pick_force_batch(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra, c->tile.prune_steps != 0);
     MDRL_TRY(prepare_force_kernel(fn, c->p.device));
     const size_t smem = force_smem_bytes(c->p.ntypes, extra, kBatchFT / 32);
@@ -410,7 +485,7 @@ extern "C" mdrl_status mdrl_batch_force_eval(mdrl_batch *b, const float *x, cons
     MDRL_CUDA(cudaEventRecord(c->ev0, c->stream));
     MDRL_TRY(batch_bin_user(b, q ? c->d_uq : nullptr, type ? c->d_ut : nullptr, 0));
     MDRL_TRY(batch_launch_force(b, c->d_pos[0], c->d_type[0], extra, c->d_F64));
-    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, 0, c->d_kepart, c->d_tot, extra ? 1 : 0);
+    k_totals<<<1, 1024, 0, c->stream>>>(batch_slots(b), c->d_unit, 0, c->d_kepart, c->d_tot, extra ? 1 : 0);
     k_unsort<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_id[0], c->d_F64, nullptr, c->d_cnt, c->d_ox, c->d_oy,
                                                   c->d_oz, counts ? c->d_ocnt : nullptr);
     MDRL_CUDA(cudaGetLastError());
@@ -455,7 +530,7 @@ extern "C" mdrl_status mdrl_batch_set_state(mdrl_batch *b, const float *x, const
     MDRL_TRY(batch_launch_force(b, c->d_pos[0], c->d_type[0], extra, c->d_F64));
     k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[0], c->d_type[0], c->d_F64, nullptr, c->d_mt, 0,
                                                 c->d_kepart);
-    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot, extra ? 1 : 0);
+    k_totals<<<1, 1024, 0, c->stream>>>(batch_slots(b), c->d_unit, nblk(n, 256), c->d_kepart, c->d_tot, extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     MDRL_CUDA(cudaStreamSynchronize(c->stream));
     MDRL_TRY(check_device_errors(c));
@@ -488,7 +563,7 @@ static mdrl_status batch_enqueue_step(mdrl_batch *b, bool extra) {
     if (vv || extra)
         k_kick<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->d_vel[d], c->d_type[d], c->d_F64, nullptr, c->d_mt,
                                                     vv ? 1 : 0, extra ? c->d_kepart : nullptr);
-    k_totals<<<1, 1024, 0, c->stream>>>(b->nitems, c->d_unit, extra ? nblk(n, 256) : 0, c->d_kepart, c->d_tot,
+    k_totals<<<1, 1024, 0, c->stream>>>(batch_slots(b), c->d_unit, extra ? nblk(n, 256) : 0, c->d_kepart, c->d_tot,
                                        extra ? 1 : 0);
     MDRL_CUDA(cudaGetLastError());
     return MDRL_OK;
@@ -563,7 +638,10 @@ extern "C" mdrl_status mdrl_batch_replica_stats(mdrl_batch *b, mdrl_stats *out) 
     MDRL_CUDA(cudaSetDevice(c->p.device));
     const int a = c->cur;
     const bool kin = c->have_state;
-    k_rep_totals<<<b->nrep, 128, 0, c->stream>>>(b->d_item_begin, b->d_rep_items, c->d_unit, b->d_reps,
+    const bool warp = c->tile.warps_per_cta == 1;
+    k_rep_totals<<<b->nrep, 128, 0, c->stream>>>(warp ? b->d_begin_ot : b->d_item_begin, warp ? b->d_list_ot : b->d_rep_items,
+                                                 warp ? b->d_begin_hs : nullptr, warp ? b->d_list_hs : nullptr, b->n_ot,
+                                                 warp ? c->tile.steps_per_piece : 1, c->d_unit, b->d_reps,
                                                  kin ? c->d_vel[a] : nullptr, c->d_type[a], c->d_mt,
                                                  b->d_reptot);
     MDRL_CUDA(cudaGetLastError());
@@ -612,7 +690,13 @@ extern "C" mdrl_status mdrl_batch_time_force(mdrl_batch *b, float *ms) {
 
 extern "C" mdrl_status mdrl_batch_set_tile(mdrl_batch *b, const mdrl_tile *t) {
     if (!b || !t) { set_error("mdrl_batch_set_tile: null argument"); return MDRL_ERR_INVALID_ARG; }
-    return set_tile(b->c, t, false);
+    const mdrl_tile before = b->c->tile;
+    MDRL_TRY(set_tile(b->c, t, false, true));
+    /* another tile lays the result slots out differently: the last evaluation's no longer apply */
+    if (before.warps_per_cta != t->warps_per_cta || before.steps_per_piece != t->steps_per_piece ||
+        before.prune_steps != t->prune_steps)
+        b->have_eval = false;
+    return MDRL_OK;
 }
 
 extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *best, float *best_ms,
@@ -625,7 +709,7 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
     snprintf(buf, sizeof buf, "batch-r%d-n%d-c%d-i%d-", b->nrep, b->ntot, b->ncells, b->nitems);
     const std::string key = std::string(buf) + tune_key_common(c);
     auto time_tile = [&](const mdrl_tile &t, float *ms) -> mdrl_status {
-        MDRL_TRY(set_tile(c, &t, false));
+        MDRL_TRY(set_tile(c, &t, false, true));
         float v[5];
         for (int r = 0; r < 5; ++r) MDRL_TRY(mdrl_batch_time_force(b, &v[r]));
         std::sort(v, v + 5);
@@ -635,7 +719,8 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
     const mdrl_tile def = {kBatchFT / 32, kStepsPerPiece, 0};
     mdrl_tile pick = def;
     float pick_ms = 0.0f, def_ms = 0.0f;
-    const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick) && pick.warps_per_cta == 4;
+    const bool cached = !(flags & MDRL_TUNE_RETIME) && tune_lookup(key, &pick) &&
+                        (pick.warps_per_cta == 4 || pick.warps_per_cta == 1);
     if (cached) {
         MDRL_TRY(time_tile(pick, &pick_ms));
         if (default_ms) MDRL_TRY(time_tile(def, &def_ms));
@@ -649,9 +734,16 @@ extern "C" mdrl_status mdrl_batch_autotune(mdrl_batch *b, int flags, mdrl_tile *
                 if (spp == def.steps_per_piece && pr == def.prune_steps) def_ms = ms;
                 if (ms < pick_ms) { pick_ms = ms; pick = t; }
             }
+        for (int grp = 1; grp <= 3; ++grp) {     /* one warp per (half-shell unit, i-tile group) */
+            const mdrl_tile t = {1, grp, 1};
+            float ms;
+            MDRL_TRY(time_tile(t, &ms));
+            if (ms < pick_ms) { pick_ms = ms; pick = t; }
+        }
         tune_store(key, pick, pick_ms);
     }
-    MDRL_TRY(set_tile(c, &pick, false));
+    MDRL_TRY(set_tile(c, &pick, false, true));
+    b->have_eval = false;   /* the timings overwrote the result slots */
     if (best) *best = pick;
     if (best_ms) *best_ms = pick_ms;
     if (default_ms) *default_ms = def_ms;

@@ -152,7 +152,9 @@ mdrl_status bonded_check_atoms(const mdrl_ctx *c, int n);
 void bonded_free(mdrl_ctx *c);
 mdrl_status upload_tables(mdrl_ctx *c);
 /* Tiles: change (re-capturing graphs), and the autotuner's process-wide cache. */
-mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8);
+/* allow8: 8-warp CTAs and pruning (fixed point, one system); allow_warp: one warp per item
+ * (fixed point) */
+mdrl_status set_tile(mdrl_ctx *c, const mdrl_tile *t, bool allow8, bool allow_warp);
 bool tune_lookup(const std::string &key, mdrl_tile *t);
 void tune_store(const std::string &key, const mdrl_tile &t, float ms);
 std::string tune_key_common(const mdrl_ctx *c);

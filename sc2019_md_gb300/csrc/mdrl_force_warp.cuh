@@ -45,15 +45,15 @@ inline size_t force_warp_smem_bytes(int ntypes) {
            sizeof(float) * 3 * kWarpJStride + sizeof(int) * kWarpJChunk + sizeof(unsigned) * 32;
 }
 
-template <int ORDER, bool SEP, bool EXTRA, int ACC, int MODE>
+/* BATCH: the items are the half-shell units of a batch's replicas, items[b / G] (replica geometry
+ * and cell offset from reps); otherwise every unit of one system, in launch order. */
+template <int ORDER, bool SEP, bool EXTRA, int ACC, int MODE, bool BATCH = false>
 __global__ void __launch_bounds__(32, 16)
 k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, const int *__restrict__ cstart,
-             Geom g, TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke, int n,
+             Geom gparam, TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke, int n,
              unsigned long long *__restrict__ F64, float *__restrict__ F32, int *__restrict__ counts,
              UnitOut *__restrict__ uout, const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps,
              int tilecfg, unsigned *__restrict__ err, int unit0) {
-    (void)items;
-    (void)reps;
     extern __shared__ float4 wsm[];
     float4 *sCoef = wsm;                                        /* [T^2] */
     float4 *sSB = sCoef + ntypes * ntypes;                      /* step boxes: [2][32] centre, half */
@@ -67,16 +67,30 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
     const bool coul = ke != 0.0f;
     const float far = 1.0e18f;
 
-    /* item -> (unit class position, home cell, group); unit0 is the first unit (home-major) of a
-     * restricted launch, whose home cells are whole */
-    const int nh = gridDim.x / (kHalfShellCells * G);
+    /* item -> (home cell, half-shell neighbour, group).  One system: unit class position first,
+     * then home cell, then group; unit0 is the first unit (home-major) of a restricted launch,
+     * whose home cells are whole.  Batch: the listed unit of a replica, its cells from coff on. */
     const int b = blockIdx.x;
-    const int fpos = b / (nh * G);
-    const int rem = b - fpos * nh * G;
-    const int hh = rem / G;
-    const int grp = rem - hh * G;
-    const int f = c_unit_order[fpos];
-    const int h = unit0 / kHalfShellCells + hh;
+    int f, h, grp, coff = 0;
+    Geom g;
+    if (BATCH) {
+        const BatchItem it = items[b / G];
+        const BatchRep rp = reps[it.rep];
+        g = rp.g;
+        coff = rp.cell_off;
+        h = it.unit / kHalfShellCells;
+        f = it.unit - h * kHalfShellCells;
+        grp = b - (b / G) * G;
+    } else {
+        g = gparam;
+        const int nh = gridDim.x / (kHalfShellCells * G);
+        const int fpos = b / (nh * G);
+        const int rem = b - fpos * nh * G;
+        const int hh = rem / G;
+        grp = rem - hh * G;
+        f = c_unit_order[fpos];
+        h = unit0 / kHalfShellCells + hh;
+    }
 
     const int nyz = g.nc[1] * g.nc[2];
     const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
@@ -89,8 +103,8 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
     cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
     const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
     const bool self = (f == 0);
-    const int hs = cstart[h], ni_all = cstart[h + 1] - hs;
-    const int cs = cstart[c], nj_all = cstart[c + 1] - cs;
+    const int hs = cstart[coff + h], ni_all = cstart[coff + h + 1] - hs;
+    const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
 
     float acc_elj = 0.0f, acc_ec = 0.0f, acc_vir = 0.0f;
     unsigned acc_pairs = 0, acc_below = 0;
@@ -318,6 +332,9 @@ force_fn pick_force_warp_set(int order, bool sep, bool extra) {
         default: return se(std::integral_constant<int, 3>{});
     }
 }
+
+/* the batched-replica set (half-shell replicas, per-unit shift) */
+force_fn pick_force_warp_batch(int order, bool sep, bool extra);
 
 extern template force_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
 extern template force_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);

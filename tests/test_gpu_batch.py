@@ -60,10 +60,15 @@ def test_batch_layout(reps):
     assert lay["total_items"] == lay["items"].sum()
 
 
-def test_batch_force_half_shell_equals_single_context(reps):
+@pytest.mark.parametrize("tile", [None, (1, 2, 1)])
+def test_batch_force_half_shell_equals_single_context(reps, tile):
+    """With the default tile and with one warp per item (half-shell replicas in the warp kernel,
+    the others in the CTA kernel), each half-shell replica equals a lone context on the same tile."""
     pos, vel, q, t, spec = systems.concat(reps)
     p = _params(reps[0], flags=m.FLAG_ENERGY)
     with m.Batch(p, spec) as b:
+        if tile is not None:
+            b.set_tile(*tile)
         F, st, cnt = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t, counts=True)
         rs = b.replica_stats()
         offs = b.offsets
@@ -72,6 +77,8 @@ def test_batch_force_half_shell_equals_single_context(reps):
         if PATHS[r] != m.PATH_HALF_SHELL:
             continue
         with m.Context(_params(s, flags=m.FLAG_ENERGY)) as ctx:
+            if tile is not None:
+                ctx.set_tile(*tile)
             F1, st1, cnt1 = ctx.force(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.q, s.type, counts=True)
         assert np.array_equal(_split(F, offs, r).view(np.uint32), F1.view(np.uint32)), f"replica {r}"
         assert np.array_equal(_split(cnt, offs, r), cnt1)
@@ -81,11 +88,13 @@ def test_batch_force_half_shell_equals_single_context(reps):
             assert abs(rs[r][key] - st1[key]) <= 1e-9 * max(abs(st1[key]), 1.0), (r, key)
 
 
-@pytest.mark.parametrize("arith", [m.ARITH_FMA, m.ARITH_SEPARATE])
-def test_batch_force_all_pairs_vs_oracle(reps, arith):
+@pytest.mark.parametrize("arith,tile", [(m.ARITH_FMA, None), (m.ARITH_SEPARATE, None), (m.ARITH_FMA, (1, 1, 1))])
+def test_batch_force_all_pairs_vs_oracle(reps, arith, tile):
     pos, vel, q, t, spec = systems.concat(reps)
     p = _params(reps[0], flags=m.FLAG_ENERGY, arith=arith)
     with m.Batch(p, spec) as b:
+        if tile is not None:
+            b.set_tile(*tile)
         F, st, cnt = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t, counts=True)
         F2, _, _ = b.force(pos[:, 0], pos[:, 1], pos[:, 2], q, t)
         rs = b.replica_stats()
@@ -109,10 +118,13 @@ def test_batch_force_all_pairs_vs_oracle(reps, arith):
     assert checked == 4
 
 
-def test_batch_md_half_shell_equals_single_context(reps):
+@pytest.mark.parametrize("tile", [None, (1, 3, 1)])
+def test_batch_md_half_shell_equals_single_context(reps, tile):
     pos, vel, q, t, spec = systems.concat(reps)
     p = _params(reps[0])
     with m.Batch(p, spec) as b:
+        if tile is not None:
+            b.set_tile(*tile)
         b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
         b.step(25)
         X, V, F = b.state()
@@ -121,6 +133,8 @@ def test_batch_md_half_shell_equals_single_context(reps):
         if PATHS[r] != m.PATH_HALF_SHELL:
             continue
         with m.Context(_params(s)) as ctx:
+            if tile is not None:
+                ctx.set_tile(*tile)
             ctx.set_state(s.pos[:, 0], s.pos[:, 1], s.pos[:, 2], s.vel, s.q, s.type)
             ctx.step(25)
             X1, V1, F1 = ctx.state()

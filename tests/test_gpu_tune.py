@@ -116,7 +116,8 @@ def test_batch_autotune_and_tile_parity():
     with m.Batch(p, spec) as b:
         b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
         r = b.autotune(retime=True)
-        assert r["tile"][0] == 4 and r["tile"][1] in (3, 4, 6, 8, 12) and r["tile"][2] in (0, 1)
+        assert (r["tile"][0] == 4 and r["tile"][1] in (3, 4, 6, 8, 12) and r["tile"][2] in (0, 1)) or \
+            (r["tile"][0] == 1 and r["tile"][1] in (1, 2, 3) and r["tile"][2] == 1)
         assert 0 < r["ms"] <= r["default_ms"]
         with pytest.raises(m.MdrlError):
             b.set_tile(8, 6)
