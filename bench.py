@@ -431,7 +431,13 @@ def sub_workload_batch(m, reps, args, local, flush, props):
     with m.Batch(params, spec) as b:
         lay = b.layout()
         b.set_state(pos[:, 0], pos[:, 1], pos[:, 2], vel, q, t)
-        tune = b.autotune(retime=True) if not args.no_tune else {"tile": (4, 6, 0), "ms": None, "default_ms": None}
+        if args.tile:
+            b.set_tile(*args.tile)
+            tune = {"tile": tuple(args.tile), "ms": None, "default_ms": None}
+        elif args.no_tune:
+            tune = {"tile": (4, 6, 0), "ms": None, "default_ms": None}
+        else:
+            tune = b.autotune(retime=True)
         leg = md_leg(m, b, k, args.warmup, flush, nkernel=5)
     with m.Batch(params, spec) as b:       # e2e: host arrays in and out (copies inside the call)
         b.set_tile(*tune["tile"])

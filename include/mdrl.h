@@ -124,10 +124,13 @@ typedef struct {
 
 typedef struct mdrl_ctx mdrl_ctx;
 
-/* Tile of the half-shell force kernel: warps per CTA (4, or 8 with MDRL_ACC_FIXED64 outside a
- * batch), j-steps of 8 particles per work piece (1..32), and whether a unit first drops the
- * (32-i, 8-j) blocks whose bounding boxes are beyond rc (exact; pays with many particles per
- * cell or cells well above rc).  Default {4, 6, 0}. */
+/* Tile of the half-shell force kernel.  Either the CTA kernel: warps per CTA (4, or 8 with
+ * MDRL_ACC_FIXED64 outside a batch), j-steps of 8 particles per work piece (1..32), and whether a
+ * unit first drops the (32-i, 8-j) blocks whose bounding boxes are beyond rc (exact; pays with
+ * many particles per cell or cells well above rc).  Or, with warps_per_cta = 1 (MDRL_ACC_FIXED64,
+ * also in batches), one warp per work item: steps_per_piece (1..4) is then the number of i-tile
+ * groups each unit is split into, and prune_steps must be 1 (the kernel always prunes).
+ * Default {4, 6, 0}; mdrl_autotune picks among both kinds. */
 typedef struct {
     int warps_per_cta;
     int steps_per_piece;
