@@ -87,11 +87,12 @@ class Clocks:
         self.proc = None
         self.lines: list[str] = []
 
-    def start(self):
+    def start(self, window: str = "0.3 s of back-to-back warm-up steps right before the timed steps, then the timed steps"):
+        self.window = window
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=self._read, daemon=True)
             self.reader.start()
@@ -138,7 +139,7 @@ class Clocks:
         loaded = [s for s, u in zip(sm, busy) if u > 0] or sm
         return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
                 "samples": len(sm), "samples_under_load": len([u for u in busy if u > 0]),
-                "window": "from the autotuner's timings through the timed steps"}
+                "window": self.window, "interval_ms": 20}
 
 
 def dist_setup(args):
@@ -349,8 +350,6 @@ def single_system(m, sysm, args, local, flush, clocks=None, barrier=lambda: None
 
     with m.Context(p_tuned) as ctx:
         ctx.set_state(*st_args)
-        if clocks is not None:
-            clocks.start()
         if args.tile:
             ctx.set_tile(*args.tile)
             tune = {"tile": ctx.tile(), "ms": None, "default_ms": None}
@@ -359,6 +358,11 @@ def single_system(m, sysm, args, local, flush, clocks=None, barrier=lambda: None
         else:
             tune = ctx.autotune(retime=True)
         ctx.step(args.warmup)
+        if clocks is not None:
+            clocks.start()     # sample the clocks under sustained load: warm-up steps back to back, then the timed steps
+            t_soak = time.perf_counter()
+            while time.perf_counter() - t_soak < 0.3:
+                ctx.step(20)
         barrier()
         t0 = time.perf_counter()
         leg = md_leg(m, ctx, args.steps, 0, flush, nkernel=max(3, min(args.steps, 20)))
@@ -632,7 +636,7 @@ def run_batch(args, rank, world, local, dist):
     gen_s = time.perf_counter() - t0
     flush = Flush(f"cuda:{local}")
     props = torch.cuda.get_device_properties(local)
-    clocks = Clocks(local).start()
+    clocks = Clocks(local).start("the whole batch run: tuning, timed steps, e2e calls, the replicas one by one")
     sub = sub_workload_batch(m, reps, args, local, flush, props)
     clk = clocks.stop()
     return {"metric": "pair-evals/s, batched replicas (one launch per kernel per step) vs one by one",

@@ -439,6 +439,8 @@ static __global__ void __launch_bounds__(1024) k_totals(int nunits, const UnitOu
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     double a = 0, b = 0, c = 0, k = 0;
     unsigned long long p = 0, q = 0;
+    /* unrolled so that the loads of several slots are in flight at once (the sums keep their order) */
+#pragma unroll 8
     for (int u = t; u < nunits; u += 1024) {
         p += uout[u].pairs;
         if (with_energy) {
@@ -446,6 +448,7 @@ static __global__ void __launch_bounds__(1024) k_totals(int nunits, const UnitOu
             q += uout[u].below;
         }
     }
+#pragma unroll 8
     for (int u = t; u < nke; u += 1024) k += kepart[u];
     const bool fp = with_energy || nke > 0;
 #pragma unroll
