@@ -462,7 +462,7 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
         const int items = force_slots(c, units);
         MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
         if (items > 0)
-            fn<<<items, 32, force_warp_smem_bytes(c->p.ntypes), c->stream>>>(
+            fn<<<items, 32, force_warp_smem_bytes(c->p.ntypes, extra), c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, n, F64, F32, c->d_cnt,
                 c->d_unit, nullptr, nullptr, c->tile.steps_per_piece, c->d_err, unit0);
         MDRL_CUDA(cudaGetLastError());

@@ -396,7 +396,7 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
                 c->d_cnt, c->d_unit, b->d_items_ot, b->d_reps, tile_word(kStepsPerPiece, 0), c->d_err, 0);
         if (b->n_hs)
-            fw<<<b->n_hs * G, 32, force_warp_smem_bytes(c->p.ntypes), c->stream>>>(
+            fw<<<b->n_hs * G, 32, force_warp_smem_bytes(c->p.ntypes, extra), c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
                 c->d_cnt, c->d_unit + b->n_ot, b->d_items_hs, b->d_reps, G, c->d_err, 0);
         MDRL_CUDA(cudaGetLastError());

@@ -701,7 +701,6 @@ k_force(const float4 *__restrict__ pos, const int *__restrict__ ptype,
     __shared__ unsigned long long s_cnt[FW][2];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int row = lane >> 3, col = lane & 7;
     int unit = blockIdx.x + unit0, coff = 0;   /* unit0: first unit of a restricted home range */
     bool cell_pair = false, use_wrap = false;
     Geom gb;

@@ -40,9 +40,12 @@ constexpr int kMaxItemGroups = 4;             /* i-tile groups per unit */
 /* Half-shell offsets in launch order: self, faces, edges, corners (indices into c_halfshell). */
 __constant__ int c_unit_order[kHalfShellCells] = {0, 1, 3, 9, 2, 4, 6, 8, 10, 12, 5, 7, 11, 13};
 
-inline size_t force_warp_smem_bytes(int ntypes) {
-    return sizeof(float4) * (size_t)(ntypes * ntypes + 2 * 32 + 2 * 8) +
-           sizeof(float) * 3 * kWarpJStride + sizeof(int) * kWarpJChunk + sizeof(unsigned) * 32;
+/* Shared memory of one item's warp: (A14, B8) per type pair, and (A12, B6) with energies; the
+ * step and group boxes; the j accumulator (and partner counts with EXTRA); the step list. */
+inline size_t force_warp_smem_bytes(int ntypes, bool extra) {
+    const size_t t2 = (size_t)((ntypes * ntypes + 1) & ~1);
+    return sizeof(float2) * t2 * (extra ? 2 : 1) + sizeof(float4) * (2 * 32 + 2 * 8) +
+           sizeof(float) * 3 * kWarpJStride + (extra ? sizeof(int) * kWarpJChunk : 0) + sizeof(unsigned) * 32;
 }
 
 /* BATCH: the items are the half-shell units of a batch's replicas, items[b / G] (replica geometry
@@ -54,13 +57,16 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
              unsigned long long *__restrict__ F64, float *__restrict__ F32, int *__restrict__ counts,
              UnitOut *__restrict__ uout, const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps,
              int tilecfg, unsigned *__restrict__ err, int unit0) {
+    constexpr int nst = kWarpJChunk / 8;                        /* steps per chunk */
+    const int t2 = (ntypes * ntypes + 1) & ~1;
     extern __shared__ float4 wsm[];
-    float4 *sCoef = wsm;                                        /* [T^2] */
-    float4 *sSB = sCoef + ntypes * ntypes;                      /* step boxes: [2][32] centre, half */
-    float4 *sGB = sSB + 2 * 32;                                 /* group boxes of the tile: [2][8] */
+    float2 *sCoefF = reinterpret_cast<float2 *>(wsm);           /* (A14, B8) [T^2] */
+    float2 *sCoefE = sCoefF + t2;                               /* (A12, B6) [T^2], EXTRA only */
+    float4 *sSB = reinterpret_cast<float4 *>(sCoefE + (EXTRA ? t2 : 0));   /* step boxes: [2][nst] centre, half */
+    float4 *sGB = sSB + 2 * nst;                                /* group boxes of the tile: [2][8] */
     float *sFj = reinterpret_cast<float *>(sGB + 2 * 8);        /* [3][kWarpJStride] */
-    int *sCj = reinterpret_cast<int *>(sFj + 3 * kWarpJStride); /* [kWarpJChunk] */
-    unsigned *sList = reinterpret_cast<unsigned *>(sCj + kWarpJChunk);   /* [32] */
+    int *sCj = reinterpret_cast<int *>(sFj + 3 * kWarpJStride); /* [kWarpJChunk], EXTRA only */
+    unsigned *sList = reinterpret_cast<unsigned *>(sCj + (EXTRA ? kWarpJChunk : 0));   /* [32] */
 
     const int lane = threadIdx.x, row = lane >> 3, col = lane & 7;
     const int G = tilecfg & 0xff;
@@ -119,7 +125,11 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
     const float margin = 9.5367431640625e-07f * fmaxf(g.L[0], fmaxf(g.L[1], g.L[2]));
 
     if (!skip) {
-        for (int t = lane; t < ntypes * ntypes; t += 32) sCoef[t] = pcoef[t];
+        for (int t = lane; t < ntypes * ntypes; t += 32) {
+            const float4 c4 = pcoef[t];
+            sCoefF[t] = make_float2(c4.x, c4.y);
+            if (EXTRA) sCoefE[t] = make_float2(c4.z, c4.w);
+        }
 
         for (int j0 = 0; j0 < nj_all; j0 += kWarpJChunk) {
             const int nj = min(kWarpJChunk, nj_all - j0);
@@ -138,7 +148,7 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
                     ux = fmaxf(ux, pp.x); uy = fmaxf(uy, pp.y); uz = fmaxf(uz, pp.z);
                 }
                 sSB[lane] = make_float4(0.5f * (lx + ux), 0.5f * (ly + uy), 0.5f * (lz + uz), 0.0f);
-                sSB[32 + lane] = make_float4(0.5f * (ux - lx), 0.5f * (uy - ly), 0.5f * (uz - lz), 0.0f);
+                sSB[nst + lane] = make_float4(0.5f * (ux - lx), 0.5f * (uy - ly), 0.5f * (uz - lz), 0.0f);
             }
             __syncwarp();
 
@@ -173,7 +183,7 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
                  * of the self unit hold no pair i < j */
                 unsigned km = 0;
                 if (lane < S && !(self && j0 + 8 * lane + 7 <= i0)) {
-                    const float4 jc = sSB[lane], jh = sSB[32 + lane];
+                    const float4 jc = sSB[lane], jh = sSB[nst + lane];
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const float4 tc = sGB[k], th = sGB[8 + k];
@@ -237,7 +247,8 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
                         if (ok) {
                             float v14, v8, v3, v12, v6, v1;
                             pair_functions_fast<ORDER, SEP, EXTRA>(tab, r2, coul, v14, v8, v3, v12, v6, v1);
-                            const float4 pc = sCoef[tti[k] + ttj];
+                            const float2 pf = sCoefF[tti[k] + ttj];
+                            const float4 pc = make_float4(pf.x, pf.y, 0.0f, 0.0f);
                             const float qq = __fmul_rn(qi[k], qj);
                             const float fs = combine_force<SEP>(pc, qq, coul, v14, v8, v3);
                             const float fx = __fmul_rn(fs, dx), fy = __fmul_rn(fs, dy), fz = __fmul_rn(fs, dz);
@@ -248,7 +259,8 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
                                 ++ci[k];
                                 ++cj;
                                 acc_below += (ORDER > 0 && r2 < tab.r2min) ? 1u : 0u;
-                                acc_elj += combine_elj<SEP>(pc, v12, v6);
+                                const float2 pe = sCoefE[tti[k] + ttj];
+                                acc_elj += combine_elj<SEP>(make_float4(0.0f, 0.0f, pe.x, pe.y), v12, v6);
                                 if (coul) acc_ec += __fmul_rn(qq, v1);
                                 acc_vir += __fmul_rn(fs, r2);
                             }

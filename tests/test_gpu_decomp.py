@@ -12,12 +12,16 @@ from sc2019_md_gb300 import systems
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("which,nranks,exact", [("small", 2, True), ("small", 5, False), ("ljc92k", 3, True)])
-def test_slab_evaluations_sum_to_the_single_domain(which, nranks, exact):
+@pytest.mark.parametrize("which,nranks,exact,tile", [("small", 2, True, None), ("small", 5, False, None),
+                                                    ("ljc92k", 3, True, None), ("small", 3, True, (1, 2, 1)),
+                                                    ("ljc92k", 2, False, (1, 1, 1))])
+def test_slab_evaluations_sum_to_the_single_domain(which, nranks, exact, tile):
     sysm = systems.small_ljc(6400, 62.5, 12.0, seed=77) if which == "small" else systems.ljc92k()
     p = sysm.params(table_order=2 if exact else 1, table_bins=512, flags=m.FLAG_EXACT_DIFF if exact else 0)
     x = sysm.pos[:, 0]
     with m.Context(p) as ctx:
+        if tile is not None:
+            ctx.set_tile(*tile)
         F_ref, st_ref = ctx.force_fixed(x, sysm.pos[:, 1], sysm.pos[:, 2], sysm.q, sysm.type)
         F = np.zeros_like(F_ref)
         pairs = 0
