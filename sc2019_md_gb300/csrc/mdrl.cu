@@ -202,7 +202,7 @@ static mdrl_status check_cells(mdrl_ctx *c) {
 mdrl_status mdrl::upload_tables(mdrl_ctx *c) {
     const int nidx = c->nseg * c->bins;
     const int nc = c->order + 1;
-    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr);
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_fp2); dfree(&c->d_fc2);
     auto coef = [&](int f, int k, int idx) { return c->tab[((size_t)f * nc + k) * nidx + idx]; };
     if (c->order == 1) {
         std::vector<float2> f2((size_t)3 * nidx), e2((size_t)3 * nidx);
@@ -230,6 +230,20 @@ mdrl_status mdrl::upload_tables(mdrl_ctx *c) {
                 f4[(size_t)3 * i + f] = make_float4(a[0], a[1], a[2], a[3]);
                 e4[(size_t)3 * i + f] = make_float4(b[0], b[1], b[2], b[3]);
             }
+        if (nc == 3) {
+            /* order 2 packed without padding for the one-warp-per-item kernel (36 bytes per index) */
+            std::vector<float4> fp2((size_t)2 * nidx);
+            std::vector<float> fc2((size_t)nidx);
+            for (int i = 0; i < nidx; ++i) {
+                fp2[(size_t)2 * i] = make_float4(coef(0, 0, i), coef(0, 1, i), coef(0, 2, i), coef(1, 0, i));
+                fp2[(size_t)2 * i + 1] = make_float4(coef(1, 1, i), coef(1, 2, i), coef(2, 0, i), coef(2, 1, i));
+                fc2[i] = coef(2, 2, i);
+            }
+            MDRL_TRY(dalloc(&c->d_fp2, fp2.size()));
+            MDRL_TRY(dalloc(&c->d_fc2, fc2.size()));
+            MDRL_CUDA(cudaMemcpy(c->d_fp2, fp2.data(), sizeof(float4) * fp2.size(), cudaMemcpyHostToDevice));
+            MDRL_CUDA(cudaMemcpy(c->d_fc2, fc2.data(), sizeof(float) * fc2.size(), cudaMemcpyHostToDevice));
+        }
         MDRL_TRY(dalloc(&c->d_f4, f4.size()));
         MDRL_TRY(dalloc(&c->d_e4, e4.size()));
         MDRL_CUDA(cudaMemcpy(c->d_f4, f4.data(), sizeof(float4) * f4.size(), cudaMemcpyHostToDevice));
@@ -251,7 +265,7 @@ mdrl_status mdrl::upload_tables(mdrl_ctx *c) {
 
 TableDev mdrl::table_dev(const mdrl_ctx *c) {
     TableDev t;
-    t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4; t.fr = c->d_fr;
+    t.f2 = c->d_f2; t.e2 = c->d_e2; t.f4 = c->d_f4; t.e4 = c->d_e4; t.fr = c->d_fr; t.fp2 = c->d_fp2; t.fc2 = c->d_fc2;
     t.order = c->order; t.nseg = c->nseg; t.bins = c->bins; t.lb = ilog2i(c->bins);
     t.min_log2 = c->min_log2;
     t.r2min = std::ldexp(1.0f, c->min_log2);
@@ -348,7 +362,8 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
     pme_free(c);
     bonded_free(c);
     free_particles(c);
-    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_pcoef);
+    dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_fp2); dfree(&c->d_fc2);
+    dfree(&c->d_pcoef);
     dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
     dfree(&c->d_tot); dfree(&c->d_err); dfree(&c->d_mt);
     if (c->h_tot) cudaFreeHost(c->h_tot);

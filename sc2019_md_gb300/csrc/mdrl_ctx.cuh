@@ -71,7 +71,8 @@ struct mdrl_ctx {
     std::vector<float> pcoef;    /* [T*T*4] */
     float ke = 0.0f;
     float2 *d_f2 = nullptr, *d_e2 = nullptr;
-    float4 *d_f4 = nullptr, *d_e4 = nullptr;
+    float4 *d_f4 = nullptr, *d_e4 = nullptr, *d_fp2 = nullptr;
+    float *d_fc2 = nullptr;
     float4 *d_fr = nullptr;      /* order 1: force functions packed per index (32 B) */
     float4 *d_pcoef = nullptr;
     MassTab mt_half, mt_full;

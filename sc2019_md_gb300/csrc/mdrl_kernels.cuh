@@ -38,6 +38,9 @@ struct TableDev {
     const float4 *f4, *e4;
     const float4 *fr;   /* order 1, force functions packed per index in one 32-byte sector:
                            {c0_14, c1_14, c0_8, c1_8}, {c0_3, c1_3, 0, 0} */
+    const float4 *fp2;  /* order 2, the force functions' 9 coefficients without padding: per index
+                           {c0_14, c1_14, c2_14, c0_8}, {c1_8, c2_8, c0_3, c1_3} ... */
+    const float *fc2;   /* ... and c2_3 */
     int order, nseg, bins, lb, min_log2;
     float r2min;
     int local;          /* orders 2-3: coefficients in u = r2 - bin start */

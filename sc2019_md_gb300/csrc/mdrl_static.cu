@@ -291,6 +291,8 @@ extern "C" mdrl_status mdrl_force_eval_static(const mdrl_params *p, int n, const
     tab.f2 = (const float2 *)(b + kLayout.tabf); tab.e2 = (const float2 *)(b + kLayout.tabe);
     tab.f4 = (const float4 *)(b + kLayout.tabf); tab.e4 = (const float4 *)(b + kLayout.tabe);
     tab.fr = (const float4 *)(b + kLayout.tabr);
+    tab.fp2 = nullptr;   /* the packed order-2 rows are read by the one-warp-per-item kernel only */
+    tab.fc2 = nullptr;
     tab.order = order; tab.nseg = nseg; tab.bins = bins;
     int lb = 0;
     while ((1 << lb) < bins) ++lb;
