@@ -272,14 +272,22 @@ def e2e_leg(m, params, sysm, tile, warmup: int, calls: int, flush):
     return {"secs": secs, "pairs": pairs, "calls": calls, "dev_ms": dev, "n": n}
 
 
-def roofline(pairs_per_launch: float, force_ms: float, n: int, props, mhz: float, capture: dict) -> dict:
+def force_kernel_name(tile, batch: bool = False) -> str:
+    if tile and tile[0] == 1:
+        return ("k_force_warp (half-shell pair force, one warp per unit x i-tile group)" if not batch else
+                "k_force_warp for the half-shell replicas + k_force for the small ones (one force evaluation)")
+    return "k_force (half-shell pair force, one CTA per unit)"
+
+
+def roofline(pairs_per_launch: float, force_ms: float, n: int, props, mhz: float, capture: dict,
+             kernel: str = "k_force (half-shell pair force)") -> dict:
     achieved = pairs_per_launch * FLOPS_PER_PAIR / (force_ms * 1e-3) / 1e12
     peak = fp32_peak_tflops(props, mhz)
     alg_bytes = n * BYTES_PER_PARTICLE
     hbm = measured_peaks().get("hbm_gbs")
     return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "traffic": capture.get("dram_bytes_per_launch") if capture.get("matched") else None,
-            "kernel": "k_force (half-shell pair force)", "force_ms": force_ms, "flops_per_pair": FLOPS_PER_PAIR,
+            "kernel": kernel, "force_ms": force_ms, "flops_per_pair": FLOPS_PER_PAIR,
             "algorithmic_bytes_per_launch": alg_bytes,
             "hbm_achieved_gbs": alg_bytes / (force_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm,
             "peak_source": f"computed: {props.multi_processor_count} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz "
@@ -416,7 +424,8 @@ def sub_workload_single(m, sysm, args, local, flush, props):
                   "force_ms": plain["force_ms"], "accumulation": "FP32 atomics, default tile, same datapath"},
         "tuned_over_plain": (plain["dev_ms"] / tuned["dev_ms"]) if tuned["dev_ms"] else None,
         "roofline": roofline(tuned["pairs_per_step"], tuned["force_ms"], sysm.n, props, mhz,
-                             ncu_capture(sysm.name, tune["tile"], args.order, args.bins, exact, sysm.table_min_log2)),
+                             ncu_capture(sysm.name, tune["tile"], args.order, args.bins, exact, sysm.table_min_log2),
+                             force_kernel_name(tune["tile"])),
         "e2e": {"value": e2e["pairs"] / e2e["secs"], "unit": "pair-evals/s", "h2d_bytes_per_step": sysm.n * 20,
                 "d2h_bytes_per_step": sysm.n * 12, "calls": e2e["calls"],
                 "ms_per_call": e2e["secs"] / e2e["calls"] * 1e3},
@@ -479,7 +488,8 @@ def sub_workload_batch(m, reps, args, local, flush, props):
                        "how": "a batch of one replica each (default tile), stepped in turn, each its own graph"},
         "batched_over_one_by_one": value / one if one else None,
         "roofline": roofline(leg["pairs_per_step"], leg["force_ms"], ntot, props, mhz,
-                             ncu_capture("batch512", tune["tile"], 1, args.bins, False, reps[0].table_min_log2)),
+                             ncu_capture("batch512", tune["tile"], 1, args.bins, False, reps[0].table_min_log2),
+                             force_kernel_name(tune["tile"], batch=True)),
         "e2e": {"value": e_pairs / e_secs, "unit": "pair-evals/s", "h2d_bytes_per_step": ntot * 20,
                 "d2h_bytes_per_step": ntot * 12, "calls": 3, "ms_per_call": e_secs / 3 * 1e3,
                 "call": "mdrl_batch_force_eval (host x,y,z,q,type in; fx,fy,fz out)"},
@@ -591,7 +601,8 @@ def run_ours(args, rank, world, local, dist):
                                "tile": tile_str(refd["tile"]), "method": method_desc(1, args.bins, False),
                                "pairs_per_step": refd["pairs_per_step"],
                                "note": "int64 fixed point, autotuned; pair list bit-equal to the reference's datapath"},
-        "roofline": roofline(tuned["pairs_per_step"], tuned["force_ms"], sysm.n, props, mhz, cap),
+        "roofline": roofline(tuned["pairs_per_step"], tuned["force_ms"], sysm.n, props, mhz, cap,
+                             force_kernel_name(tuned["tile"])),
         "e2e": {"value": sm[1] / mx[1], "unit": "pair-evals/s", "h2d_bytes_per_step": sysm.n * 20,
                 "d2h_bytes_per_step": sysm.n * 12,
                 "call": "mdrl_force_eval (pinned host x,y,z,q,type in; fx,fy,fz out)", "calls": e2e["calls"],
