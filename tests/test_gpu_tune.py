@@ -56,6 +56,36 @@ def test_tile_parity_and_reproducibility(sysm, tile, grid, exact):
     assert err.max() <= 1.0, err.max()
 
 
+@pytest.mark.parametrize("tile", [(1, 1, 1), (1, 3, 1)])
+@pytest.mark.parametrize("order,arith,exact", [(0, m.ARITH_FMA, False), (0, m.ARITH_FMA, True),
+                                               (1, m.ARITH_SEPARATE, False), (2, m.ARITH_SEPARATE, False),
+                                               (3, m.ARITH_FMA, False), (3, m.ARITH_FMA, True)])
+def test_warp_tile_every_evaluation_mode(sysm, tile, order, arith, exact):
+    """The one-warp-per-item kernel for every table order (0 = direct evaluation), both arithmetic
+    modes of the reference's difference rule and the exact rule: partner counts and pair totals
+    exact, forces within the parity bound, energies within 1e-5, bit-reproducible."""
+    kw = dict(table_bins=512, arith=arith, flags=m.FLAG_ENERGY | (m.FLAG_EXACT_DIFF if exact else 0))
+    if order == 0:
+        kw["eval"] = m.EVAL_DIRECT
+    else:
+        kw["table_order"] = order
+    p = sysm.params(**kw)
+    x, y, z = (np.ascontiguousarray(sysm.pos[:, k]) for k in range(3))
+    with m.Context(p) as ctx:
+        ctx.set_tile(*tile)
+        F, st, cnt = ctx.force(x, y, z, sysm.q, sysm.type, counts=True)
+        F2, _, _ = ctx.force(x, y, z, sysm.q, sysm.type)
+        o = oracle_from_ctx(ctx, sysm)
+    Fo, Fabs, cnto, sto = o.force_cells()
+    assert np.array_equal(cnt, cnto)
+    assert st["pairs"] == sto["pairs"]
+    assert np.array_equal(F.view(np.uint32), F2.view(np.uint32))
+    err = np.abs(F - Fo) / (SUM_TOL * Fabs + FIX_ABS)
+    assert err.max() <= 1.0, err.max()
+    for key in ("e_lj", "e_coul", "virial"):
+        assert abs(st[key] - sto[key]) <= 1e-5 * max(abs(sto[key]), 1.0), (key, st[key], sto[key])
+
+
 def test_autotune_picks_a_candidate_and_caches(sysm):
     p = sysm.params(table_bins=512)
     args = (sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
