@@ -25,7 +25,15 @@
  * global sums are exact.
  *
  * Items are launched face-class first (self, the 3 face neighbours, 6 edges, 4 corners), so the
- * small corner units finish the launch and the block scheduler balances the SMs.
+ * small corner units finish the launch and the block scheduler balances the SMs.  In a batch the
+ * items are the half-shell units of the replicas with at least 3 cells per axis, from the batch's
+ * cost-ordered list.
+ *
+ * L1 footprint.  The force table and the cells' particles are read through L1, which shares its
+ * 256 KB with the shared memory of the 16 resident CTAs, so each CTA keeps only what it must in
+ * shared memory (force multipliers as float2; energy multipliers and partner counts only in
+ * energy launches) and order-2 rows are read from a packed 36-byte copy of the table: on the
+ * 1M-atom system (16 types) this raised the L1 hit rate from 66 % to 91 %.
  */
 #pragma once
 
