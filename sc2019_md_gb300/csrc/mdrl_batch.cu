@@ -158,9 +158,10 @@ struct mdrl_batch {
     BatchRep *d_reps = nullptr;
     BatchItem *d_items = nullptr;
     int *d_rep_of = nullptr, *d_item_begin = nullptr, *d_rep_items = nullptr;
-    /* the same work split for one-warp-per-item tiles: half-shell items (warp kernel) and the
-     * others (the CTA kernel), each in cost order, with per-replica lists */
-    int n_hs = 0, n_ot = 0;
+    /* the same work split for one-warp-per-item tiles: the warp kernel's list (n_cp explicit cell
+     * pairs, then n_hs half-shell units) and the all-image blocks (the CTA kernel), each in cost
+     * order, with per-replica lists */
+    int n_hs = 0, n_cp = 0, n_ot = 0;
     BatchItem *d_items_hs = nullptr, *d_items_ot = nullptr;
     int *d_begin_hs = nullptr, *d_list_hs = nullptr, *d_begin_ot = nullptr, *d_list_ot = nullptr;
     RepTotals *d_reptot = nullptr;
@@ -310,10 +311,15 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
         for (int k = 0; k < bt->nitems; ++k) bt->rep_items[fill[bt->items[k].rep]++] = k;
     }
     /* the split for one-warp-per-item tiles (cost order kept within each list) */
-    std::vector<BatchItem> items_hs, items_ot;
-    for (const BatchItem &it : bt->items) (hrep[it.rep].path == kPathHalfShell ? items_hs : items_ot).push_back(it);
+    std::vector<BatchItem> items_hs, items_cp, items_ot;
+    for (const BatchItem &it : bt->items) {
+        const int path = hrep[it.rep].path;
+        (path == kPathHalfShell ? items_hs : (path == kPathMinImage ? items_cp : items_ot)).push_back(it);
+    }
     bt->n_hs = (int)items_hs.size();
+    bt->n_cp = (int)items_cp.size();
     bt->n_ot = (int)items_ot.size();
+    items_hs.insert(items_hs.begin(), items_cp.begin(), items_cp.end());   /* the warp list: pairs, then units */
     auto rep_lists = [&](const std::vector<BatchItem> &v, std::vector<int> &begin, std::vector<int> &list) {
         begin.assign(nrep + 1, 0);
         for (const BatchItem &it : v) begin[it.rep + 1]++;
@@ -336,7 +342,8 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
     c->ncells = bt->ncells;
     if ((s = dalloc(&c->d_count, (size_t)bt->ncells)) != MDRL_OK) return fail(s);
     if ((s = dalloc(&c->d_start, (size_t)bt->ncells + 1)) != MDRL_OK) return fail(s);
-    if ((s = dalloc(&c->d_unit, std::max((size_t)bt->nitems, (size_t)bt->n_ot + (size_t)bt->n_hs * kMaxItemGroups))) != MDRL_OK)
+    if ((s = dalloc(&c->d_unit, std::max((size_t)bt->nitems,
+                                         (size_t)bt->n_ot + ((size_t)bt->n_cp + bt->n_hs) * kMaxItemGroups))) != MDRL_OK)
         return fail(s);
     if ((s = ensure_capacity(c, bt->ntot)) != MDRL_OK) return fail(s);
     std::vector<int> rep_of(bt->ntot);
@@ -359,11 +366,13 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_rep_of, rep_of.data(), sizeof(int) * bt->ntot, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_item_begin, bt->item_begin.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_rep_items, bt->rep_items.data(), sizeof(int) * bt->nitems, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && bt->n_hs) e = cudaMemcpy(bt->d_items_hs, items_hs.data(), sizeof(BatchItem) * bt->n_hs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !items_hs.empty())
+        e = cudaMemcpy(bt->d_items_hs, items_hs.data(), sizeof(BatchItem) * items_hs.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && bt->n_ot) e = cudaMemcpy(bt->d_items_ot, items_ot.data(), sizeof(BatchItem) * bt->n_ot, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_begin_hs, begin_hs.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_begin_ot, begin_ot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && bt->n_hs) e = cudaMemcpy(bt->d_list_hs, list_hs.data(), sizeof(int) * bt->n_hs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !list_hs.empty())
+        e = cudaMemcpy(bt->d_list_hs, list_hs.data(), sizeof(int) * list_hs.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && bt->n_ot) e = cudaMemcpy(bt->d_list_ot, list_ot.data(), sizeof(int) * bt->n_ot, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         set_error(std::string("mdrl_batch_create: ") + cudaGetErrorString(e));
@@ -375,30 +384,38 @@ extern "C" mdrl_status mdrl_batch_create(const mdrl_params *p, int nrep, const m
 
 /* Result slots of a batch force launch (one per CTA). */
 static int batch_slots(const mdrl_batch *b) {
-    return b->c->tile.warps_per_cta == 1 ? b->n_ot + b->n_hs * b->c->tile.steps_per_piece : b->nitems;
+    return b->c->tile.warps_per_cta == 1 ? b->n_ot + (b->n_cp + b->n_hs) * b->c->tile.steps_per_piece : b->nitems;
 }
 
 static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const int *type, bool extra,
                                       unsigned long long *F64) {
     mdrl_ctx *c = b->c;
     if (c->tile.warps_per_cta == 1) {
-        /* the replicas with fewer than 3 cells per axis in the CTA kernel (default tile), then the
-         * half-shell units one warp per (unit, i-tile group) */
+        /* the replicas with an edge of at most 2 rc in the CTA kernel (every periodic image,
+         * default tile), then one warp per (item, i-tile group): the explicit cell pairs of the
+         * other small replicas (per-pair wrap), then the half-shell units */
         const bool sep = c->p.arith == MDRL_ARITH_SEPARATE;
         force_fn fo = pick_force_batch(eff_order(c), sep, extra, false);
-        force_fn fw = pick_force_warp_batch(eff_order(c), sep, extra);
+        force_fn fp = pick_force_warp_batch(eff_order(c), sep, extra, true);
+        force_fn fw = pick_force_warp_batch(eff_order(c), sep, extra, false);
         MDRL_TRY(prepare_force_kernel(fo, c->p.device));
+        MDRL_TRY(prepare_force_kernel(fp, c->p.device));
         MDRL_TRY(prepare_force_kernel(fw, c->p.device));
         const int G = c->tile.steps_per_piece;
+        const size_t wsm = force_warp_smem_bytes(c->p.ntypes, extra);
         MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
         if (b->n_ot)
             fo<<<b->n_ot, kBatchFT, force_smem_bytes(c->p.ntypes, extra, kBatchFT / 32), c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
                 c->d_cnt, c->d_unit, b->d_items_ot, b->d_reps, tile_word(kStepsPerPiece, 0), c->d_err, 0);
-        if (b->n_hs)
-            fw<<<b->n_hs * G, 32, force_warp_smem_bytes(c->p.ntypes, extra), c->stream>>>(
+        if (b->n_cp)
+            fp<<<b->n_cp * G, 32, wsm, c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
                 c->d_cnt, c->d_unit + b->n_ot, b->d_items_hs, b->d_reps, G, c->d_err, 0);
+        if (b->n_hs)
+            fw<<<b->n_hs * G, 32, wsm, c->stream>>>(
+                pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
+                c->d_cnt, c->d_unit + b->n_ot + (size_t)b->n_cp * G, b->d_items_hs + b->n_cp, b->d_reps, G, c->d_err, 0);
         MDRL_CUDA(cudaGetLastError());
         MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
         return MDRL_OK;

@@ -106,18 +106,27 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
 
     /* item -> (home cell, half-shell neighbour, group).  One system: unit class position first,
      * then home cell, then group; unit0 is the first unit (home-major) of a restricted launch,
-     * whose home cells are whole.  Batch: the listed unit of a replica, its cells from coff on. */
+     * whose home cells are whole.  Batch: the listed unit of a replica, its cells from coff on;
+     * with the per-pair wrap (MODE kDiffWrap) the unit is an explicit pair of the replica's cells
+     * (a * cells + b, a <= b) of a box whose edges all exceed 2 rc. */
+    constexpr bool kCellPair = BATCH && MODE == kDiffWrap;
     const int b = blockIdx.x;
-    int f, h, grp, coff = 0;
+    int f = 0, h, grp, coff = 0, cpair = 0;
     Geom g;
     if (BATCH) {
         const BatchItem it = items[b / G];
         const BatchRep rp = reps[it.rep];
         g = rp.g;
         coff = rp.cell_off;
-        h = it.unit / kHalfShellCells;
-        f = it.unit - h * kHalfShellCells;
         grp = b - (b / G) * G;
+        if (kCellPair) {
+            const int nct = g.nc[0] * g.nc[1] * g.nc[2];
+            h = it.unit / nct;
+            cpair = it.unit - h * nct;
+        } else {
+            h = it.unit / kHalfShellCells;
+            f = it.unit - h * kHalfShellCells;
+        }
     } else {
         g = gparam;
         const int nh = gridDim.x / (kHalfShellCells * G);
@@ -132,14 +141,15 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
     const int nyz = g.nc[1] * g.nc[2];
     const int hx = h / nyz, hy = (h / g.nc[2]) % g.nc[1], hz = h % g.nc[2];
     int cx = hx + c_halfshell[f][0], cy = hy + c_halfshell[f][1], cz = hz + c_halfshell[f][2];
-    const float sx = cx >= g.nc[0] ? -g.L[0] : (cx < 0 ? g.L[0] : 0.0f);
-    const float sy = cy >= g.nc[1] ? -g.L[1] : (cy < 0 ? g.L[1] : 0.0f);
-    const float sz = cz >= g.nc[2] ? -g.L[2] : (cz < 0 ? g.L[2] : 0.0f);
+    /* the unit's periodic shift (none for explicit cell pairs, which wrap per pair) */
+    const float sx = kCellPair ? 0.0f : (cx >= g.nc[0] ? -g.L[0] : (cx < 0 ? g.L[0] : 0.0f));
+    const float sy = kCellPair ? 0.0f : (cy >= g.nc[1] ? -g.L[1] : (cy < 0 ? g.L[1] : 0.0f));
+    const float sz = kCellPair ? 0.0f : (cz >= g.nc[2] ? -g.L[2] : (cz < 0 ? g.L[2] : 0.0f));
     cx = cx < 0 ? cx + g.nc[0] : (cx >= g.nc[0] ? cx - g.nc[0] : cx);
     cy = cy < 0 ? cy + g.nc[1] : (cy >= g.nc[1] ? cy - g.nc[1] : cy);
     cz = cz < 0 ? cz + g.nc[2] : (cz >= g.nc[2] ? cz - g.nc[2] : cz);
-    const int c = (cx * g.nc[1] + cy) * g.nc[2] + cz;
-    const bool self = (f == 0);
+    const int c = kCellPair ? cpair : (cx * g.nc[1] + cy) * g.nc[2] + cz;
+    const bool self = kCellPair ? (h == cpair) : (f == 0);
     const int hs = cstart[coff + h], ni_all = cstart[coff + h + 1] - hs;
     const int cs = cstart[coff + c], nj_all = cstart[coff + c + 1] - cs;
 
@@ -218,9 +228,13 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const float4 tc = sGB[k], th = sGB[8 + k];
-                        const float gx = fmaxf(fabsf(tc.x - jc.x) - (th.x + jh.x), 0.0f);
-                        const float gy = fmaxf(fabsf(tc.y - jc.y) - (th.y + jh.y), 0.0f);
-                        const float gz = fmaxf(fabsf(tc.z - jc.z) - (th.z + jh.z), 0.0f);
+                        float ex = tc.x - jc.x, ey = tc.y - jc.y, ez = tc.z - jc.z;
+                        if (MODE == kDiffWrap) {   /* the centres' minimum image */
+                            ex = wrap_d(ex, g.L[0], g.h[0]); ey = wrap_d(ey, g.L[1], g.h[1]); ez = wrap_d(ez, g.L[2], g.h[2]);
+                        }
+                        const float gx = fmaxf(fabsf(ex) - (th.x + jh.x), 0.0f);
+                        const float gy = fmaxf(fabsf(ey) - (th.y + jh.y), 0.0f);
+                        const float gz = fmaxf(fabsf(ez) - (th.z + jh.z), 0.0f);
                         if (th.x >= 0.0f && gx * gx + gy * gy + gz * gz <= g.rc2) km |= 1u << k;
                     }
                 }
@@ -376,8 +390,9 @@ force_fn pick_force_warp_set(int order, bool sep, bool extra) {
     }
 }
 
-/* the batched-replica set (half-shell replicas, per-unit shift) */
-force_fn pick_force_warp_batch(int order, bool sep, bool extra);
+/* the batched-replica sets: half-shell replicas (per-unit shift), and explicit cell pairs of
+ * replicas with fewer than 3 cells per axis but every edge above 2 rc (per-pair wrap) */
+force_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs);
 
 extern template force_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
 extern template force_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);

@@ -1,17 +1,20 @@
 /*
  * mdrl_force_warp_batch.cu — the one-warp-per-item force-kernel instantiations for batches: the
- * half-shell units of the replicas that have at least 3 cells per axis, int64 fixed point, the
- * per-unit shift; one translation unit so that the set compiles in parallel with the others.
+ * half-shell units of the replicas that have at least 3 cells per axis (per-unit shift), and the
+ * explicit cell pairs of the replicas whose edges all exceed 2 rc with fewer cells (per-pair
+ * wrap); int64 fixed point; one translation unit so that the sets compile in parallel with the
+ * others.
  */
 #include "mdrl_force_warp.cuh"
 
 namespace mdrl {
 
-force_fn pick_force_warp_batch(int order, bool sep, bool extra) {
+force_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs) {
     auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return (force_fn)k_force_warp<O, S, E, 0, kDiffShift, true>;
+        return cell_pairs ? (force_fn)k_force_warp<O, S, E, 0, kDiffWrap, true>
+                          : (force_fn)k_force_warp<O, S, E, 0, kDiffShift, true>;
     };
     auto se = [&](auto ord) -> force_fn {
         using T = std::true_type;
