@@ -364,7 +364,7 @@ extern "C" mdrl_status mdrl_destroy(mdrl_ctx *c) {
     free_particles(c);
     dfree(&c->d_f2); dfree(&c->d_e2); dfree(&c->d_f4); dfree(&c->d_e4); dfree(&c->d_fr); dfree(&c->d_fp2); dfree(&c->d_fc2);
     dfree(&c->d_pcoef);
-    dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart);
+    dfree(&c->d_count); dfree(&c->d_start); dfree(&c->d_unit); dfree(&c->d_kepart); dfree(&c->d_work);
     dfree(&c->d_tot); dfree(&c->d_err); dfree(&c->d_mt);
     if (c->h_tot) cudaFreeHost(c->h_tot);
     if (c->h_err) cudaFreeHost(c->h_err);
@@ -385,6 +385,7 @@ static mdrl_status ensure_cells(mdrl_ctx *c) {
     MDRL_TRY(dalloc(&c->d_count, c->ncells));
     MDRL_TRY(dalloc(&c->d_start, c->ncells + 1));
     MDRL_TRY(dalloc(&c->d_unit, (size_t)c->ncells * kHalfShellCells * kMaxItemGroups));
+    MDRL_TRY(dalloc(&c->d_work, 1));
     return MDRL_OK;
 }
 
@@ -471,15 +472,21 @@ static mdrl_status launch_force_into(mdrl_ctx *c, int n, const float4 *pos, cons
     if (c->tile.warps_per_cta == 1) {
         /* one warp per (unit, i-tile group); fixed point only (set_tile checks) */
         const bool exact = (c->p.flags & MDRL_FLAG_EXACT_DIFF) != 0;
-        force_fn fn = exact ? pick_force_warp_set<0, kDiffExact>(eff_order(c), false, extra)
-                            : pick_force_warp_set<0, kDiffShift>(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra);
-        MDRL_TRY(prepare_force_kernel(fn, c->p.device));
+        warp_fn fn = exact ? pick_force_warp_set<0, kDiffExact>(eff_order(c), false, extra)
+                           : pick_force_warp_set<0, kDiffShift>(eff_order(c), c->p.arith == MDRL_ARITH_SEPARATE, extra);
+        MDRL_TRY(prepare_force_kernel((force_fn)fn, c->p.device));
         const int items = force_slots(c, units);
+        const size_t smem = force_warp_smem_bytes(c->p.ntypes, extra);
+        /* a persistent grid: the CTAs that fit at once take items from the counter */
+        int per_sm = 0;
+        MDRL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)fn, 32, smem));
+        const int grid = std::min(items, std::max(1, per_sm) * std::max(1, c->num_sms));
+        if (items > 0) MDRL_CUDA(cudaMemsetAsync(c->d_work, 0, sizeof(int), c->stream));
         MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
         if (items > 0)
-            fn<<<items, 32, force_warp_smem_bytes(c->p.ntypes, extra), c->stream>>>(
+            fn<<<grid, 32, smem, c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, n, F64, F32, c->d_cnt,
-                c->d_unit, nullptr, nullptr, c->tile.steps_per_piece, c->d_err, unit0);
+                c->d_unit, nullptr, nullptr, c->tile.steps_per_piece, c->d_err, unit0, c->d_work, items);
         MDRL_CUDA(cudaGetLastError());
         MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
         return MDRL_OK;

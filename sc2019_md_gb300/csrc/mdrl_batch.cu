@@ -396,11 +396,11 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
          * other small replicas (per-pair wrap), then the half-shell units */
         const bool sep = c->p.arith == MDRL_ARITH_SEPARATE;
         force_fn fo = pick_force_batch(eff_order(c), sep, extra, false);
-        force_fn fp = pick_force_warp_batch(eff_order(c), sep, extra, true);
-        force_fn fw = pick_force_warp_batch(eff_order(c), sep, extra, false);
+        warp_fn fp = pick_force_warp_batch(eff_order(c), sep, extra, true);
+        warp_fn fw = pick_force_warp_batch(eff_order(c), sep, extra, false);
         MDRL_TRY(prepare_force_kernel(fo, c->p.device));
-        MDRL_TRY(prepare_force_kernel(fp, c->p.device));
-        MDRL_TRY(prepare_force_kernel(fw, c->p.device));
+        MDRL_TRY(prepare_force_kernel((force_fn)fp, c->p.device));
+        MDRL_TRY(prepare_force_kernel((force_fn)fw, c->p.device));
         const int G = c->tile.steps_per_piece;
         const size_t wsm = force_warp_smem_bytes(c->p.ntypes, extra);
         MDRL_CUDA(cudaEventRecord(c->evf0, c->stream));
@@ -411,11 +411,12 @@ static mdrl_status batch_launch_force(mdrl_batch *b, const float4 *pos, const in
         if (b->n_cp)
             fp<<<b->n_cp * G, 32, wsm, c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
-                c->d_cnt, c->d_unit + b->n_ot, b->d_items_hs, b->d_reps, G, c->d_err, 0);
+                c->d_cnt, c->d_unit + b->n_ot, b->d_items_hs, b->d_reps, G, c->d_err, 0, nullptr, 0);
         if (b->n_hs)
             fw<<<b->n_hs * G, 32, wsm, c->stream>>>(
                 pos, type, c->d_start, c->g, table_dev(c), c->d_pcoef, c->p.ntypes, c->ke, b->ntot, F64, nullptr,
-                c->d_cnt, c->d_unit + b->n_ot + (size_t)b->n_cp * G, b->d_items_hs + b->n_cp, b->d_reps, G, c->d_err, 0);
+                c->d_cnt, c->d_unit + b->n_ot + (size_t)b->n_cp * G, b->d_items_hs + b->n_cp, b->d_reps, G, c->d_err, 0,
+                nullptr, 0);
         MDRL_CUDA(cudaGetLastError());
         MDRL_CUDA(cudaEventRecord(c->evf1, c->stream));
         return MDRL_OK;

@@ -91,6 +91,7 @@ struct mdrl_ctx {
     int cur = 0;
     int *d_cell_of = nullptr, *d_slot = nullptr, *d_tmp = nullptr, *d_sorted = nullptr;
     int *d_count = nullptr, *d_start = nullptr;
+    int *d_work = nullptr;      /* the persistent warp kernel's item counter */
     unsigned *d_key = nullptr;   /* in-cell sort key (Morton code inside the cell) */
     unsigned long long *d_sortkey = nullptr;   /* sorted chunks of cells above kSortSmall */
     unsigned long long *d_F64 = nullptr;

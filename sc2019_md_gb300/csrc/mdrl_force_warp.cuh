@@ -24,8 +24,10 @@
  * xor tree), the item decomposition does not depend on scheduling, and the int64 fixed-point
  * global sums are exact.
  *
- * Items are launched face-class first (self, the 3 face neighbours, 6 edges, 4 corners), so the
- * small corner units finish the launch and the block scheduler balances the SMs.  In a batch the
+ * Items are taken face-class first (self, the 3 face neighbours, 6 edges, 4 corners), so the
+ * small corner units finish the launch.  For one system the grid is persistent: as many 32-thread
+ * CTAs as fit on the GPU at once, each taking the next item from a counter (an atomic per item)
+ * until none is left, so no slot waits for the block scheduler between items.  In a batch the
  * items are the half-shell units of the replicas with at least 3 cells per axis, from the batch's
  * cost-ordered list.
  *
@@ -79,6 +81,12 @@ inline size_t force_warp_smem_bytes(int ntypes, bool extra) {
            sizeof(float) * 3 * kWarpJStride + (extra ? sizeof(int) * kWarpJChunk : 0) + sizeof(unsigned) * 32;
 }
 
+/* The warp kernel's launch signature: force_fn plus the persistent grid's item counter (zero at
+ * launch) and item count (work == nullptr: one item per CTA, blockIdx.x). */
+typedef void (*warp_fn)(const float4 *, const int *, const int *, Geom, TableDev, const float4 *, int, float,
+                        int, unsigned long long *, float *, int *, UnitOut *, const BatchItem *,
+                        const BatchRep *, int, unsigned *, int, int *, int);
+
 /* BATCH: the items are the half-shell units of a batch's replicas, items[b / G] (replica geometry
  * and cell offset from reps); otherwise every unit of one system, in launch order. */
 template <int ORDER, bool SEP, bool EXTRA, int ACC, int MODE, bool BATCH = false>
@@ -87,7 +95,7 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
              Geom gparam, TableDev tab, const float4 *__restrict__ pcoef, int ntypes, float ke, int n,
              unsigned long long *__restrict__ F64, float *__restrict__ F32, int *__restrict__ counts,
              UnitOut *__restrict__ uout, const BatchItem *__restrict__ items, const BatchRep *__restrict__ reps,
-             int tilecfg, unsigned *__restrict__ err, int unit0) {
+             int tilecfg, unsigned *__restrict__ err, int unit0, int *__restrict__ work, int nitems) {
     constexpr int nst = kWarpJChunk / 8;                        /* steps per chunk */
     const int t2 = (ntypes * ntypes + 1) & ~1;
     extern __shared__ float4 wsm[];
@@ -110,7 +118,14 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
      * with the per-pair wrap (MODE kDiffWrap) the unit is an explicit pair of the replica's cells
      * (a * cells + b, a <= b) of a box whose edges all exceed 2 rc. */
     constexpr bool kCellPair = BATCH && MODE == kDiffWrap;
-    const int b = blockIdx.x;
+    const int total = work ? nitems : (int)gridDim.x;
+    int bfirst = blockIdx.x;
+    if (work) {
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(work, 1);
+        bfirst = __shfl_sync(0xffffffffu, t0, 0);
+    }
+    for (int b = bfirst; b < total;) {   /* one item per pass; one pass without a counter */
     int f = 0, h, grp, coff = 0, cpair = 0;
     Geom g;
     if (BATCH) {
@@ -129,7 +144,7 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
         }
     } else {
         g = gparam;
-        const int nh = gridDim.x / (kHalfShellCells * G);
+        const int nh = total / (kHalfShellCells * G);
         const int fpos = b / (nh * G);
         const int rem = b - fpos * nh * G;
         const int hh = rem / G;
@@ -365,18 +380,24 @@ k_force_warp(const float4 *__restrict__ pos, const int *__restrict__ ptype, cons
         u.pairs = c1; u.below = c2;
         uout[b] = u;
     }
+    if (!work) break;
+    __syncwarp();   /* this item's shared-memory reads are done before the next item writes */
+    int t1 = 0;
+    if (lane == 0) t1 = atomicAdd(work, 1);
+    b = __shfl_sync(0xffffffffu, t1, 0);
+    }
 }
 
 /* One set: every order x extra (x arithmetic mode for the reference's difference rule; the exact
  * rule is instantiated with fused arithmetic only). */
 template <int ACC, int DIFF>
-force_fn pick_force_warp_set(int order, bool sep, bool extra) {
-    auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
+warp_fn pick_force_warp_set(int order, bool sep, bool extra) {
+    auto w = [&](auto ord, auto sp, auto ex) -> warp_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return (force_fn)k_force_warp<O, S, E, ACC, DIFF>;
+        return k_force_warp<O, S, E, ACC, DIFF>;
     };
-    auto se = [&](auto ord) -> force_fn {
+    auto se = [&](auto ord) -> warp_fn {
         using T = std::true_type;
         using F = std::false_type;
         if (DIFF == kDiffShift && sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});
@@ -392,9 +413,9 @@ force_fn pick_force_warp_set(int order, bool sep, bool extra) {
 
 /* the batched-replica sets: half-shell replicas (per-unit shift), and explicit cell pairs of
  * replicas with fewer than 3 cells per axis but every edge above 2 rc (per-pair wrap) */
-force_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs);
+warp_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs);
 
-extern template force_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
-extern template force_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);
+extern template warp_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
+extern template warp_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);
 
 }  // namespace mdrl

@@ -9,14 +9,14 @@
 
 namespace mdrl {
 
-force_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs) {
-    auto w = [&](auto ord, auto sp, auto ex) -> force_fn {
+warp_fn pick_force_warp_batch(int order, bool sep, bool extra, bool cell_pairs) {
+    auto w = [&](auto ord, auto sp, auto ex) -> warp_fn {
         constexpr int O = decltype(ord)::value;
         constexpr bool S = decltype(sp)::value, E = decltype(ex)::value;
-        return cell_pairs ? (force_fn)k_force_warp<O, S, E, 0, kDiffWrap, true>
-                          : (force_fn)k_force_warp<O, S, E, 0, kDiffShift, true>;
+        return cell_pairs ? (warp_fn)k_force_warp<O, S, E, 0, kDiffWrap, true>
+                          : (warp_fn)k_force_warp<O, S, E, 0, kDiffShift, true>;
     };
-    auto se = [&](auto ord) -> force_fn {
+    auto se = [&](auto ord) -> warp_fn {
         using T = std::true_type;
         using F = std::false_type;
         if (sep) return extra ? w(ord, T{}, T{}) : w(ord, T{}, F{});

@@ -7,6 +7,6 @@
 
 namespace mdrl {
 
-template force_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
+template warp_fn pick_force_warp_set<0, kDiffShift>(int, bool, bool);
 
 }  // namespace mdrl

@@ -7,6 +7,6 @@
 
 namespace mdrl {
 
-template force_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);
+template warp_fn pick_force_warp_set<0, kDiffExact>(int, bool, bool);
 
 }  // namespace mdrl

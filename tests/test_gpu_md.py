@@ -38,10 +38,15 @@ def _vv_reference(sysm, ctx, F0, dt, nsteps):
     return x, v, F
 
 
-def test_step_matches_reference_integration():
+@pytest.mark.parametrize("tile", [None, (1, 1, 1)])
+def test_step_matches_reference_integration(tile):
+    """Three velocity-Verlet steps (one captured graph each) against numpy integration with oracle
+    forces, with the default tile and with the persistent one-warp-per-item kernel."""
     sysm = systems.lj1728()
     p = sysm.params(table_bins=512)
     with m.Context(p) as ctx:
+        if tile is not None:
+            ctx.set_tile(*tile)
         ctx.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, None, sysm.type)
         x0, v0, F0 = ctx.state()
         st = ctx.step(3)
@@ -80,12 +85,17 @@ def test_step_energy_conservation_liquid_argon():
     assert drift < 1e-2 * np.abs(e[:, 1]).mean(), (drift, e[:, 1].mean())
 
 
-def test_step_deterministic():
+@pytest.mark.parametrize("tile", [None, (1, 2, 1)])
+def test_step_deterministic(tile):
+    """Two runs of 7 steps are bit-identical (with the persistent warp kernel, whichever warp takes
+    an item computes it the same way)."""
     sysm = systems.small_ljc(2500, 37.5, 12.0, seed=31)
     p = sysm.params(table_bins=512)
     out = []
     for _ in range(2):
         with m.Context(p) as ctx:
+            if tile is not None:
+                ctx.set_tile(*tile)
             ctx.set_state(sysm.pos[:, 0], sysm.pos[:, 1], sysm.pos[:, 2], sysm.vel, sysm.q, sysm.type)
             ctx.step(7)
             out.append(ctx.state())
