@@ -76,7 +76,7 @@ def tile_str(t) -> str:
 
 
 class Clocks:
-    """nvidia-smi samples every 200 ms while running (SM clock, max clock, throttle reasons)."""
+    """nvidia-smi samples every 20 ms while running (SM clock, max clock, throttle reasons)."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
